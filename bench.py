@@ -1,0 +1,349 @@
+"""Benchmark: cell-updates/s of the RK3 advance on one periodic box.
+
+Workload (default): 128^3 cells + 4 ghost cells a side, FP64 plain form, the CNS_NoSpec
+initial field with a seeded +-1e-3 perturbation of rho, u, v, w; a step is one full RK3
+step (new_advance, cpu/advance.cpp:13-154) of that box.  The mixed FP32/FP64 form is timed on
+the same box in the same run and its error against the FP64 result is reported.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank advances its own replica box on its own GPU (the box does
+not shard: replicas only); the host-side barrier and the max over ranks go through
+torch.distributed (gloo).  Rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic FP64 work of one cell-update (one cell, one full RK3 step) in the reference's
+# formulation (each +, -, *, / one flop): 3 x (ctoprim 16 + hypterm 358 + diffterm 415)
+# + RK combines 15 + 30 + 30 + Courant 8 = 2450.
+FLOPS_PER_CELL_UPDATE = 2450
+# Of that, per cell and launch: k_deriv does the nine first derivatives (9 x 12) and the
+# dissipation terms of diffterm's energy component (24) = 132; k_assemble the rest of a stage.
+FLOPS_DERIV = 132
+FLOPS_ASSEMBLE_PER_STEP = FLOPS_PER_CELL_UPDATE - 3 * FLOPS_DERIV  # 2054 over 3 launches
+# Compulsory HBM traffic of one cell-update with the FP64 state: stage 1 reads U^n and writes
+# U^1 (80 B); stages 2 and 3 read U^(k), U^n and write U^(k+1) (120 B each).
+BYTES_PER_CELL_UPDATE = 320
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n", type=int, default=128, help="cells per axis of the periodic box")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    return p.parse_args()
+
+
+# ---- distributed plumbing (host side only) ---------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks -------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=10)
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pinned_like(shape):
+    """A pinned host float64 array when torch is importable (plumbing only), else pageable."""
+    try:
+        import torch
+        t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+        return t.numpy(), True, t
+    except Exception:
+        return np.empty(shape, dtype=np.float64), False, None
+
+
+def measured_traffic(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, scaled by cells."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        per_cell = t[kernel]["dram_bytes_per_cell"]
+        return per_cell * n ** 3, t[kernel].get("source")
+    except Exception:
+        return None, None
+
+
+# ---- CPU baseline: the oracle (the reference's algorithm restated in C) on the host cores ----
+def cpu_baseline(n: int, seconds: float):
+    from cns_nospec_gb300 import initdata as I
+    from oracle import oracle as O
+    O.build(ref=os.path.isdir(O.REF_SRC))
+    which = "ref" if (O.have_ref() and os.path.isdir(O.REF_SRC)) else "port"
+    threads = O.set_threads(os.cpu_count() or 1)
+    U = I.initial_state(n, perturb=1e-3, seed=1)
+    dx = I.box_dx(n)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which="port")
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 100:
+            break
+    return {"value": n ** 3 * steps / el, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} RK3 step(s) of the {n}^3 box, {threads} OpenMP threads, {el:.1f} s",
+            "reference_lib_present": which == "ref"}
+
+
+def run_reference(args, dist):
+    """--impl reference: the reference algorithm (the oracle port; the reference's own objects
+    cannot be rebuilt where its source tree is absent) on the host cores, same workload."""
+    if dist.rank != 0:
+        return None
+    from cns_nospec_gb300 import initdata as I
+    from oracle import oracle as O
+    O.build(ref=os.path.isdir(O.REF_SRC))
+    use_ref = O.have_ref() and os.path.isdir(O.REF_SRC)
+    threads = O.set_threads(os.cpu_count() or 1)
+    n = args.n
+    U = I.initial_state(n, perturb=1e-3, seed=1)
+    dx = I.box_dx(n)
+    which = "ref" if use_ref else "port"
+    if use_ref:
+        threads = 1  # the reference's cpu/ path is single-threaded (its OpenMP pragmas are commented out)
+    for _ in range(min(args.warmup, 1)):
+        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
+    # bounded sample: at most ~120 s of timed work
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < args.steps:
+        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
+        steps += 1
+        if time.perf_counter() - t0 > 120.0:
+            break
+    el = time.perf_counter() - t0
+    v = n ** 3 * steps / el
+    kind = "reference" if use_ref else "port"
+    return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"periodic box {n}^3 + 4 ghosts, FP64 RK3 (cpu/ path algorithm)", "n": n,
+                       "host_threads": threads},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind,
+                             "sample": f"{steps} RK3 steps of the {n}^3 box on the host cores"},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_ours(args, dist):
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    from cns_nospec_gb300 import build as B
+    from cns_nospec_gb300 import initdata as I
+    B.build()
+    lib = C.load()
+    L.check(lib.cns_set_device(dist.local))
+    n = args.n
+    dx = I.box_dx(n)
+    U0 = I.initial_state(n, perturb=1e-3, seed=1)
+
+    fp64_peak = C._lib.C.c_double(0.0)
+    L.check(lib.cns_measure_fp64_peak(C._lib.C.byref(fp64_peak)))
+    fp64_peak = fp64_peak.value
+
+    # ---- device-resident FP64 plain form: the headline value --------------------------------
+    box = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_FP64)
+    box.upload(U0)
+    box.advance_timed(args.warmup)
+    lib.cns_device_synchronize()
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        lib.cns_device_synchronize()
+        kms, klaunch, total_ms = box.advance_timed(args.steps)
+        lib.cns_device_synchronize()
+    dist.barrier()
+    box.sync()
+    t_max = dist.max(total_ms)
+    cells = n ** 3
+    value = dist.world * cells * args.steps / (t_max * 1e-3)
+    U64 = box.download()
+    box.close()
+
+    # ---- mixed form on the same box ----------------------------------------------------------
+    mbox = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_MIXED)
+    mbox.upload(U0)
+    mbox.advance_timed(args.warmup)
+    mms, _, mtotal = mbox.advance_timed(args.steps)
+    mbox.sync()
+    Umix = mbox.download()
+    mbox.close()
+    mixed_err = I.normwise_error(Umix, U64)[0]
+    mixed_value = cells * args.steps / (mtotal * 1e-3)
+
+    # ---- end to end through the reference-facing C ABI: host buffers, copies timed ----------
+    h = C.read_configurations(n, dx, I.CFL, I.ETA, I.ALAM)
+    Uh, pinned, _keep = pinned_like(U0.shape)
+    Uh[...] = U0
+    k_e2e = max(1, min(args.steps, 20))
+    C.new_advance(Uh, None, None, None, None, h)  # warm (allocates the cached device state)
+    Uh[...] = U0
+    lib.cns_device_synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        C.new_advance(Uh, None, None, None, None, h)
+    lib.cns_device_synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    dist.barrier()
+    e2e_value = dist.world * cells * k_e2e / e2e_s
+    io_bytes = int(Uh.nbytes)
+
+    # ---- roofline of the dominant kernel ----------------------------------------------------
+    names = L.KERNEL_NAMES
+    dom = int(np.argmax(kms))
+    dom_launch_ms = kms[dom] / max(klaunch[dom], 1)
+    if names[dom] == "k_assemble":
+        flops_launch = FLOPS_ASSEMBLE_PER_STEP / 3.0 * cells
+    else:
+        flops_launch = FLOPS_DERIV * cells
+    achieved_tf = flops_launch / (dom_launch_ms * 1e-3) / 1e12
+    traffic, tsrc = measured_traffic(names[dom], n)
+    step_ms = t_max / args.steps
+    hbm_gbs = BYTES_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    launches_per_step = sum(klaunch) / args.steps
+
+    result = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"periodic box {n}^3 + 4 ghosts, FP64 plain RK3 (config 1 field, seed 1)",
+                   "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
+                   "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)"},
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes, "api": "cns_new_advance (host U, copy in + 1 step + copy out)",
+                "pinned_host": pinned, "steps": k_e2e},
+        "roofline": {"bound": "fp64", "kernel": names[dom], "achieved": achieved_tf, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak,
+                     "peak_source": "measured live: FP64 FMA probe kernel (cns_measure_fp64_peak)",
+                     "flops_per_launch": flops_launch, "launch_ms": dom_launch_ms,
+                     "traffic": traffic, "traffic_source": tsrc},
+        "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak, "frac": hbm_gbs / hbm_peak,
+                "bytes_per_cell_update": BYTES_PER_CELL_UPDATE, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "fp64_step": {"achieved_tflops": FLOPS_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e12,
+                      "frac_of_fp64_peak": FLOPS_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e12 / fp64_peak},
+        "kernels_ms_per_step": {names[i]: kms[i] / args.steps for i in range(L.KERN_COUNT)},
+        "mixed": {"value": mixed_value, "unit": "cell-updates/s", "speedup_vs_fp64": mixed_value / (value / dist.world),
+                  "max_normwise_err_vs_fp64": float(mixed_err.max()),
+                  "err_per_var": [float(x) for x in mixed_err], "steps": args.steps,
+                  "kernels_ms_per_step": {names[i]: mms[i] / args.steps for i in range(L.KERN_COUNT)}},
+        "gpu_launches": int(sum(klaunch)),
+        "launches_per_step": launches_per_step,
+        "clocks": clk.summary(),
+    }
+    return result
+
+
+def Box_bytes(C, n):
+    return C.Box.bytes_for(n, C.CNS_FP64)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            res = run_reference(args, dist)
+        else:
+            res = run_ours(args, dist)
+            if dist.rank == 0 and res is not None and not args.no_cpu_baseline:
+                res["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)
+        if dist.rank == 0 and res is not None:
+            print(json.dumps(res))
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,844 @@
+// cns_capi.cu -- the C ABI (include/cns_gb300.h): device-resident boxes and batches, the
+// reference's host-array entry points, graphs and launch accounting.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cns_gb300.h"
+#include "cns_common.cuh"
+#include "cns_internal.h"
+
+using namespace cns;
+
+// ---- errors ------------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+static int fail_cuda(cudaError_t e, const char* what, int line) {
+    int code = (e == cudaErrorMemoryAllocation) ? CNS_ERR_NOMEM
+               : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? CNS_ERR_NODEVICE
+                                                                                : CNS_ERR_CUDA;
+    return fail(code, "%s failed at cns_capi.cu:%d: %s", what, line, cudaGetErrorString(e));
+}
+#define CK(call)                                                             \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) return fail_cuda(e_, #call, __LINE__);        \
+    } while (0)
+
+extern "C" const char* cns_last_error(void) { return g_err.c_str(); }
+extern "C" int cns_version(void) { return 100; }
+extern "C" int cns_set_device(int device) {
+    CK(cudaSetDevice(device));
+    return CNS_OK;
+}
+extern "C" int cns_device_synchronize(void) {
+    CK(cudaDeviceSynchronize());
+    return CNS_OK;
+}
+extern "C" int cns_measure_fp64_peak(double* tflops) {
+    if (!tflops) return fail(CNS_ERR_INVALID, "null argument");
+    CK(probe_fp64(tflops));
+    return CNS_OK;
+}
+
+// ---- geometry and coefficients ----------------------------------------------------------
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Geometry {
+    int pk;
+    long long sj, si, fs;
+    size_t off_sc, off_dtlog, off_U, off_Us, off_P0, off_P1, off_S, off_view, off_tiles, off_aos, total;
+    int ntiles;
+};
+
+static int validate_desc(const cns_box_desc* d) {
+    if (!d) return fail(CNS_ERR_INVALID, "null box description");
+    for (int a = 0; a < 3; a++) {
+        if (d->n[a] < CNS_NG) return fail(CNS_ERR_INVALID, "n[%d]=%d: each axis needs >= %d interior cells", a, d->n[a], CNS_NG);
+        if (d->n[a] > 4096) return fail(CNS_ERR_CAPACITY, "n[%d]=%d above 4096", a, d->n[a]);
+        if (!(d->dx[a] > 0.0) || !std::isfinite(d->dx[a])) return fail(CNS_ERR_INVALID, "dx[%d] must be positive", a);
+    }
+    if (!(d->cfl > 0.0)) return fail(CNS_ERR_INVALID, "cfl must be positive");
+    if (!(d->eta >= 0.0) || !(d->alam >= 0.0)) return fail(CNS_ERR_INVALID, "eta and alam must be >= 0");
+    if (d->precision != CNS_FP64 && d->precision != CNS_MIXED) return fail(CNS_ERR_INVALID, "precision must be 0 or 1");
+    return CNS_OK;
+}
+
+static Geometry geometry(const cns_box_desc* d) {
+    Geometry g;
+    int ti, tj, tk;
+    tile_shape(&ti, &tj, &tk);
+    const long long g0 = d->n[0] + 2 * CNS_NG, g1 = d->n[1] + 2 * CNS_NG, g2 = d->n[2] + 2 * CNS_NG;
+    g.pk = (int)((g2 + 7) / 8 * 8);
+    g.sj = g.pk;
+    g.si = g1 * g.sj;
+    g.fs = g0 * g.si;
+    const size_t esz = d->precision == CNS_MIXED ? 4 : 8;
+    g.ntiles = ((d->n[0] + ti - 1) / ti) * ((d->n[1] + tj - 1) / tj) * ((d->n[2] + tk - 1) / tk);
+    size_t o = 0;
+    g.off_sc = o;      o = align256(o + sizeof(BoxScalars));
+    g.off_dtlog = o;   o = align256(o + sizeof(double) * DTLOG_CAP);
+    g.off_U = o;       o = align256(o + sizeof(double) * 5 * g.fs);
+    g.off_Us = o;      o = align256(o + sizeof(double) * 5 * g.fs);
+    g.off_P0 = o;      o = align256(o + esz * NPF * g.fs);
+    g.off_P1 = o;      o = align256(o + esz * NPF * g.fs);
+    g.off_S = o;       o = align256(o + esz * NSF * g.fs);
+    g.off_view = o;    o = align256(o + sizeof(BoxView));
+    g.off_tiles = o;   o = align256(o + sizeof(Tile) * g.ntiles);
+    g.off_aos = o;     o = align256(o + sizeof(double) * CNS_NC * g0 * g1 * g2);
+    g.total = o;
+    return g;
+}
+
+template <class R>
+static void cast_coefs(CoefT<R>& dst, const CoefT<double>& s) {
+    const double* a = (const double*)&s;
+    R* b = (R*)&dst;
+    for (size_t i = 0; i < sizeof(CoefT<double>) / sizeof(double); i++) b[i] = (R)a[i];
+}
+
+static void fill_coefs(BoxView& v, const cns_box_desc* d) {
+    const double A[4] = {kAlp, kBet, kGam, kDel};
+    const double B[4] = {kOff1, kOff2, kOff3, kOff4};
+    const double dxi[3] = {1.0 / d->dx[0], 1.0 / d->dx[1], 1.0 / d->dx[2]};
+    CoefT<double>& c = v.c64;
+    memset(&c, 0, sizeof c);
+    double tsum = 0.0;
+    for (int a = 0; a < 3; a++) {
+        for (int m = 0; m < 4; m++) {
+            c.da[a][m] = A[m] * dxi[a];
+            c.ha[a][m] = -A[m] * dxi[a];
+            c.mx[a][m] = (d->eta * (1.0 / 3.0)) * A[m] * dxi[a];
+            c.tl[a][m] = d->alam * B[m] * (dxi[a] * dxi[a]);
+        }
+        tsum += dxi[a] * dxi[a];
+        c.cour[a] = dxi[a];
+    }
+    c.tc = d->alam * kCenter * tsum;
+    for (int comp = 0; comp < 3; comp++) {
+        double sum = 0.0;
+        for (int a = 0; a < 3; a++) {
+            const double w = d->eta * (comp == a ? 4.0 / 3.0 : 1.0) * (dxi[a] * dxi[a]);
+            for (int m = 0; m < 4; m++) c.vl[comp][a][m] = w * B[m];
+            sum += w;
+        }
+        c.vc[comp] = kCenter * sum;
+    }
+    c.eta = d->eta;
+    cast_coefs(v.c32, v.c64);
+}
+
+// ---- boxes -------------------------------------------------------------------------------
+struct cns_batch;
+
+struct cns_box {
+    int dev = 0;
+    cns_box_desc desc{};
+    Geometry geo{};
+    BoxView view{};
+    BoxView* d_view = nullptr;
+    Tile* d_tiles = nullptr;
+    double* d_aos = nullptr;
+    BoxScalars* d_sc = nullptr;
+    char* arena = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    bool primed = false;
+    cudaGraphExec_t gexec = nullptr;
+    cns_batch* batch = nullptr;
+};
+
+extern "C" long long cns_box_bytes(const cns_box_desc* desc) {
+    if (validate_desc(desc) != CNS_OK) return -1;
+    return (long long)geometry(desc).total;
+}
+
+extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
+    if (!out) return fail(CNS_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    int rc = validate_desc(desc);
+    if (rc) return rc;
+    cns_box* b = new (std::nothrow) cns_box();
+    if (!b) return fail(CNS_ERR_NOMEM, "host allocation failed");
+    b->desc = *desc;
+    b->geo = geometry(desc);
+    cudaError_t e = cudaGetDevice(&b->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->arena, b->geo.total);
+    if (e != cudaSuccess) {
+        if (b->own_stream) cudaStreamDestroy(b->own_stream);
+        delete b;
+        return fail_cuda(e, "cns_box_create", __LINE__);
+    }
+    b->stream = b->own_stream;
+    const Geometry& g = b->geo;
+    BoxView& v = b->view;
+    memset(&v, 0, sizeof v);
+    for (int a = 0; a < 3; a++) v.n[a] = desc->n[a];
+    v.pk = g.pk;
+    v.sj = g.sj;
+    v.si = g.si;
+    v.fs = g.fs;
+    v.U = (double*)(b->arena + g.off_U);
+    v.Us = (double*)(b->arena + g.off_Us);
+    v.P[0] = b->arena + g.off_P0;
+    v.P[1] = b->arena + g.off_P1;
+    v.S = b->arena + g.off_S;
+    v.sc = (BoxScalars*)(b->arena + g.off_sc);
+    v.dtlog = (double*)(b->arena + g.off_dtlog);
+    v.cfl = desc->cfl;
+    v.precision = desc->precision;
+    fill_coefs(v, desc);
+    b->d_view = (BoxView*)(b->arena + g.off_view);
+    b->d_tiles = (Tile*)(b->arena + g.off_tiles);
+    b->d_aos = (double*)(b->arena + g.off_aos);
+    b->d_sc = v.sc;
+    int ti, tj, tk;
+    tile_shape(&ti, &tj, &tk);
+    std::vector<Tile> tiles;
+    tiles.reserve(g.ntiles);
+    for (int i0 = 0; i0 < desc->n[0]; i0 += ti)
+        for (int j0 = 0; j0 < desc->n[1]; j0 += tj)
+            for (int k0 = 0; k0 < desc->n[2]; k0 += tk) tiles.push_back(Tile{0, i0, j0, k0});
+    e = cudaMemsetAsync(b->arena, 0, g.total, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_view, &v, sizeof v, cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        cudaFree(b->arena);
+        cudaStreamDestroy(b->own_stream);
+        delete b;
+        return fail_cuda(e, "cns_box_create init", __LINE__);
+    }
+    *out = b;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_remove(cns_batch* batch, cns_box* box);
+
+extern "C" int cns_box_destroy(cns_box* b) {
+    if (!b) return CNS_OK;
+    cudaSetDevice(b->dev);
+    if (b->batch) cns_batch_remove(b->batch, b);
+    cudaStreamSynchronize(b->stream);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    cudaFree(b->arena);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    delete b;
+    return CNS_OK;
+}
+
+extern "C" int cns_box_set_stream(cns_box* b, void* stream) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    b->stream = stream ? (cudaStream_t)stream : b->own_stream;
+    return CNS_OK;
+}
+
+// Prime a box whose U interior was just written: primitives/fluxes, Courant, first dt.
+static int prime(cns_box* b) {
+    CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
+    CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->geo.ntiles, b->stream));
+    CK(launch_stepend(b->d_view, 1, 0, b->stream));
+    b->primed = true;
+    return CNS_OK;
+}
+
+static size_t aos_bytes(const cns_box* b) {
+    return sizeof(double) * CNS_NC * (size_t)(b->desc.n[0] + 8) * (b->desc.n[1] + 8) * (b->desc.n[2] + 8);
+}
+
+extern "C" int cns_box_upload_device(cns_box* b, const double* U_dev) {
+    if (!b || !U_dev) return fail(CNS_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(b->dev));
+    CK(op_aos_to_box(U_dev, b->view, b->stream));
+    return prime(b);
+}
+
+extern "C" int cns_box_upload(cns_box* b, const double* U_host) {
+    if (!b || !U_host) return fail(CNS_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(b->dev));
+    CK(cudaMemcpyAsync(b->d_aos, U_host, aos_bytes(b), cudaMemcpyHostToDevice, b->stream));
+    int rc = cns_box_upload_device(b, b->d_aos);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    return CNS_OK;
+}
+
+extern "C" int cns_box_download_device(cns_box* b, double* U_dev) {
+    if (!b || !U_dev) return fail(CNS_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(b->dev));
+    CK(op_box_to_aos(b->view, U_dev, 1, b->stream));
+    return CNS_OK;
+}
+
+extern "C" int cns_box_download(cns_box* b, double* U_host) {
+    if (!b || !U_host) return fail(CNS_ERR_INVALID, "null argument");
+    int rc = cns_box_download_device(b, b->d_aos);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(U_host, b->d_aos, aos_bytes(b), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return CNS_OK;
+}
+
+// One RK3 step of the boxes behind `views` (tiles split by stencil precision).  When `ev`
+// is given, an event is recorded after every launch and the launch's kind appended to `kinds`.
+static int enqueue_step(const BoxView* views, int nviews, const Tile* t64, int n64, const Tile* t32, int n32,
+                        cudaStream_t st, std::vector<cudaEvent_t>* ev, std::vector<int>* kinds) {
+    auto mark = [&](int kind) -> int {
+        if (!ev) return CNS_OK;
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(e, st));
+        ev->push_back(e);
+        kinds->push_back(kind);
+        return CNS_OK;
+    };
+    int rc;
+    for (int stage = 1; stage <= 3; stage++) {
+        if (n64) {
+            CK(launch_deriv(0, views, t64, n64, stage, st));
+            if ((rc = mark(CNS_KERN_DERIV))) return rc;
+        }
+        if (n32) {
+            CK(launch_deriv(1, views, t32, n32, stage, st));
+            if ((rc = mark(CNS_KERN_DERIV))) return rc;
+        }
+        if (n64) {
+            CK(launch_assemble(0, views, t64, n64, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
+        if (n32) {
+            CK(launch_assemble(1, views, t32, n32, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
+    }
+    CK(launch_stepend(views, nviews, 1, st));
+    return mark(CNS_KERN_STEPEND);
+}
+
+static int box_tiles(const cns_box* b, const Tile** t64, int* n64, const Tile** t32, int* n32) {
+    if (b->desc.precision == CNS_MIXED) {
+        *t64 = nullptr, *n64 = 0, *t32 = b->d_tiles, *n32 = b->geo.ntiles;
+    } else {
+        *t64 = b->d_tiles, *n64 = b->geo.ntiles, *t32 = nullptr, *n32 = 0;
+    }
+    return CNS_OK;
+}
+
+static int capture_step(cudaStream_t st, cudaGraphExec_t* out, const BoxView* views, int nviews, const Tile* t64,
+                        int n64, const Tile* t32, int n32) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(views, nviews, t64, n64, t32, n32, st, nullptr, nullptr);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture", __LINE__);
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate", __LINE__);
+    return CNS_OK;
+}
+
+extern "C" int cns_box_launches_per_step(const cns_box* b) { return b ? 7 : 0; }
+
+extern "C" int cns_box_advance(cns_box* b, int nsteps) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    if (nsteps < 0) return fail(CNS_ERR_INVALID, "nsteps < 0");
+    if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
+    CK(cudaSetDevice(b->dev));
+    const Tile *t64, *t32;
+    int n64, n32;
+    box_tiles(b, &t64, &n64, &t32, &n32);
+    if (!b->gexec) {
+        int rc = capture_step(b->own_stream, &b->gexec, b->d_view, 1, t64, n64, t32, n32);
+        if (rc) return rc;
+    }
+    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(b->gexec, b->stream));
+    return CNS_OK;
+}
+
+static int timed_run(cudaStream_t st, int nsteps, const BoxView* views, int nviews, const Tile* t64, int n64,
+                     const Tile* t32, int n32, double* kernel_ms, int* kernel_launches, double* total_ms) {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kinds;
+    ev.reserve(8 * nsteps + 1);
+    kinds.reserve(8 * nsteps + 1);
+    cudaEvent_t e0;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventRecord(e0, st));
+    int rc = CNS_OK;
+    for (int s = 0; s < nsteps && rc == CNS_OK; s++) rc = enqueue_step(views, nviews, t64, n64, t32, n32, st, &ev, &kinds);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == CNS_OK && e != cudaSuccess) rc = fail_cuda(e, "cudaStreamSynchronize", __LINE__);
+    if (rc == CNS_OK) {
+        for (int k = 0; k < CNS_KERN_COUNT; k++) {
+            if (kernel_ms) kernel_ms[k] = 0.0;
+            if (kernel_launches) kernel_launches[k] = 0;
+        }
+        cudaEvent_t prev = e0;
+        for (size_t i = 0; i < ev.size(); i++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, prev, ev[i]);
+            if (kernel_ms) kernel_ms[kinds[i]] += ms;
+            if (kernel_launches) kernel_launches[kinds[i]] += 1;
+            prev = ev[i];
+        }
+        if (total_ms) {
+            float ms = 0.f;
+            if (!ev.empty()) cudaEventElapsedTime(&ms, e0, ev.back());
+            *total_ms = ms;
+        }
+    }
+    for (auto x : ev) cudaEventDestroy(x);
+    cudaEventDestroy(e0);
+    return rc;
+}
+
+extern "C" int cns_box_advance_timed(cns_box* b, int nsteps, double* kernel_ms, int* kernel_launches,
+                                     double* total_ms) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    if (nsteps < 0) return fail(CNS_ERR_INVALID, "nsteps < 0");
+    if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
+    CK(cudaSetDevice(b->dev));
+    const Tile *t64, *t32;
+    int n64, n32;
+    box_tiles(b, &t64, &n64, &t32, &n32);
+    return timed_run(b->stream, nsteps, b->d_view, 1, t64, n64, t32, n32, kernel_ms, kernel_launches, total_ms);
+}
+
+static int read_scalars(cns_box* b, BoxScalars* hs) {
+    CK(cudaMemcpyAsync(hs, b->d_sc, sizeof *hs, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return CNS_OK;
+}
+
+extern "C" int cns_box_sync(cns_box* b, int* health_bits) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    CK(cudaSetDevice(b->dev));
+    BoxScalars hs;
+    int rc = read_scalars(b, &hs);
+    if (rc) return rc;
+    if (health_bits) *health_bits = hs.status;
+    if (hs.status) return fail(CNS_ERR_NONFINITE, "box state went bad (health bits 0x%x)", hs.status);
+    return CNS_OK;
+}
+
+extern "C" int cns_box_last_dt(cns_box* b, double* dt, int* nsteps_done) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    CK(cudaSetDevice(b->dev));
+    BoxScalars hs;
+    int rc = read_scalars(b, &hs);
+    if (rc) return rc;
+    if (dt) *dt = hs.dt_last;
+    if (nsteps_done) *nsteps_done = hs.nsteps_done;
+    return CNS_OK;
+}
+
+// ---- batches -----------------------------------------------------------------------------
+struct cns_batch {
+    int dev = 0;
+    std::vector<cns_box*> members;
+    BoxView* d_views = nullptr;
+    Tile* d_tiles = nullptr;
+    size_t cap_views = 0, cap_tiles = 0;
+    int n64 = 0, n32 = 0;
+    cudaStream_t stream = nullptr, own_stream = nullptr;
+    bool dirty = true;
+    cudaGraphExec_t gexec = nullptr;
+};
+
+extern "C" int cns_batch_create(cns_batch** out) {
+    if (!out) return fail(CNS_ERR_INVALID, "null output handle");
+    cns_batch* bt = new (std::nothrow) cns_batch();
+    if (!bt) return fail(CNS_ERR_NOMEM, "host allocation failed");
+    cudaError_t e = cudaGetDevice(&bt->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bt->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete bt;
+        return fail_cuda(e, "cns_batch_create", __LINE__);
+    }
+    bt->stream = bt->own_stream;
+    *out = bt;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_destroy(cns_batch* bt) {
+    if (!bt) return CNS_OK;
+    cudaSetDevice(bt->dev);
+    cudaStreamSynchronize(bt->stream);
+    for (auto* b : bt->members) b->batch = nullptr;
+    if (bt->gexec) cudaGraphExecDestroy(bt->gexec);
+    cudaFree(bt->d_views);
+    cudaFree(bt->d_tiles);
+    if (bt->own_stream) cudaStreamDestroy(bt->own_stream);
+    delete bt;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_set_stream(cns_batch* bt, void* stream) {
+    if (!bt) return fail(CNS_ERR_INVALID, "null batch");
+    bt->stream = stream ? (cudaStream_t)stream : bt->own_stream;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_add(cns_batch* bt, cns_box* b) {
+    if (!bt || !b) return fail(CNS_ERR_INVALID, "null argument");
+    if (b->batch) return fail(CNS_ERR_INVALID, "box already belongs to a batch");
+    if (b->dev != bt->dev) return fail(CNS_ERR_INVALID, "box and batch live on different devices");
+    if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
+    bt->members.push_back(b);
+    b->batch = bt;
+    bt->dirty = true;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_remove(cns_batch* bt, cns_box* b) {
+    if (!bt || !b) return fail(CNS_ERR_INVALID, "null argument");
+    auto it = std::find(bt->members.begin(), bt->members.end(), b);
+    if (it == bt->members.end()) return fail(CNS_ERR_INVALID, "box is not in this batch");
+    bt->members.erase(it);
+    b->batch = nullptr;
+    bt->dirty = true;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->members.size() : 0; }
+
+static int batch_rebuild(cns_batch* bt) {
+    CK(cudaStreamSynchronize(bt->stream));
+    std::vector<BoxView> views;
+    std::vector<Tile> tiles64, tiles32;
+    int ti, tj, tk;
+    tile_shape(&ti, &tj, &tk);
+    for (size_t m = 0; m < bt->members.size(); m++) {
+        const cns_box* b = bt->members[m];
+        views.push_back(b->view);
+        auto& dst = b->desc.precision == CNS_MIXED ? tiles32 : tiles64;
+        for (int i0 = 0; i0 < b->desc.n[0]; i0 += ti)
+            for (int j0 = 0; j0 < b->desc.n[1]; j0 += tj)
+                for (int k0 = 0; k0 < b->desc.n[2]; k0 += tk) dst.push_back(Tile{(int)m, i0, j0, k0});
+    }
+    const size_t nt = tiles64.size() + tiles32.size();
+    if (views.size() > bt->cap_views) {
+        cudaFree(bt->d_views);
+        bt->d_views = nullptr;
+        bt->cap_views = std::max<size_t>(views.size(), 2 * bt->cap_views);
+        CK(cudaMalloc((void**)&bt->d_views, sizeof(BoxView) * bt->cap_views));
+    }
+    if (nt > bt->cap_tiles) {
+        cudaFree(bt->d_tiles);
+        bt->d_tiles = nullptr;
+        bt->cap_tiles = std::max<size_t>(nt, 2 * bt->cap_tiles);
+        CK(cudaMalloc((void**)&bt->d_tiles, sizeof(Tile) * bt->cap_tiles));
+    }
+    if (!views.empty()) CK(cudaMemcpy(bt->d_views, views.data(), sizeof(BoxView) * views.size(), cudaMemcpyHostToDevice));
+    if (!tiles64.empty()) CK(cudaMemcpy(bt->d_tiles, tiles64.data(), sizeof(Tile) * tiles64.size(), cudaMemcpyHostToDevice));
+    if (!tiles32.empty())
+        CK(cudaMemcpy(bt->d_tiles + tiles64.size(), tiles32.data(), sizeof(Tile) * tiles32.size(), cudaMemcpyHostToDevice));
+    bt->n64 = (int)tiles64.size();
+    bt->n32 = (int)tiles32.size();
+    if (bt->gexec) {
+        cudaGraphExecDestroy(bt->gexec);
+        bt->gexec = nullptr;
+    }
+    if (!views.empty()) {
+        int rc = capture_step(bt->own_stream, &bt->gexec, bt->d_views, (int)views.size(), bt->d_tiles, bt->n64,
+                              bt->d_tiles + bt->n64, bt->n32);
+        if (rc) return rc;
+    }
+    bt->dirty = false;
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_advance(cns_batch* bt, int nsteps) {
+    if (!bt) return fail(CNS_ERR_INVALID, "null batch");
+    if (nsteps < 0) return fail(CNS_ERR_INVALID, "nsteps < 0");
+    CK(cudaSetDevice(bt->dev));
+    if (bt->dirty) {
+        int rc = batch_rebuild(bt);
+        if (rc) return rc;
+    }
+    if (!bt->gexec) return CNS_OK;
+    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(bt->gexec, bt->stream));
+    return CNS_OK;
+}
+
+extern "C" int cns_batch_sync(cns_batch* bt) {
+    if (!bt) return fail(CNS_ERR_INVALID, "null batch");
+    CK(cudaSetDevice(bt->dev));
+    CK(cudaStreamSynchronize(bt->stream));
+    return CNS_OK;
+}
+
+// ---- the reference's host-array entry points ---------------------------------------------
+// A per-thread device workspace for the operator-level calls (grow-only).
+struct Workspace {
+    void* p = nullptr;
+    size_t n = 0;
+    int dev = -1;
+    cudaStream_t st = nullptr;
+    ~Workspace() {
+        if (p) cudaFree(p);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+static thread_local Workspace g_ws;
+
+static int workspace(size_t bytes, void** out, cudaStream_t* st) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (g_ws.dev != dev) {
+        if (g_ws.p) cudaFree(g_ws.p);
+        if (g_ws.st) cudaStreamDestroy(g_ws.st);
+        g_ws.p = nullptr;
+        g_ws.n = 0;
+        g_ws.st = nullptr;
+        g_ws.dev = dev;
+        CK(cudaStreamCreateWithFlags(&g_ws.st, cudaStreamNonBlocking));
+    }
+    if (bytes > g_ws.n) {
+        if (g_ws.p) cudaFree(g_ws.p);
+        g_ws.p = nullptr;
+        g_ws.n = 0;
+        CK(cudaMalloc(&g_ws.p, bytes));
+        g_ws.n = bytes;
+    }
+    *out = g_ws.p;
+    *st = g_ws.st;
+    return CNS_OK;
+}
+
+static int check_bounds(const int lo[3], const int hi[3], int ng) {
+    if (!lo || !hi) return fail(CNS_ERR_INVALID, "null lo/hi");
+    if (ng < CNS_NG) return fail(CNS_ERR_INVALID, "ng=%d: the 8th-order stencils need ng >= %d", ng, CNS_NG);
+    for (int a = 0; a < 3; a++)
+        if (hi[a] < lo[a]) return fail(CNS_ERR_INVALID, "hi[%d] < lo[%d]", a, a);
+    return CNS_OK;
+}
+
+extern "C" int cns_ctoprim(const int lo[3], const int hi[3], const double* u, double* q, const double dx[3], int ng,
+                           double* courno) {
+    int rc = check_bounds(lo, hi, ng);
+    if (rc) return rc;
+    if (!u || !q || !dx) return fail(CNS_ERR_INVALID, "null array");
+    long long np = 1;
+    for (int a = 0; a < 3; a++) np *= (hi[a] - lo[a] + 1 + 2 * ng);
+    const size_t need = sizeof(double) * (size_t)np * (5 + 5 + 6 + 6) + 256;
+    void* ws;
+    cudaStream_t st;
+    if ((rc = workspace(need, &ws, &st))) return rc;
+    double* d_aos_u = (double*)ws;
+    double* d_u = d_aos_u + 5 * np;
+    double* d_q = d_u + 5 * np;
+    double* d_aos_q = d_q + 6 * np;
+    unsigned long long* d_c = (unsigned long long*)(d_aos_q + 6 * np);
+    CK(cudaMemcpyAsync(d_aos_u, u, sizeof(double) * 5 * np, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(d_c, 0, sizeof(unsigned long long), st));
+    CK(op_aos_to_soa(d_aos_u, d_u, np, 5, st));
+    CK(op_ctoprim(lo, hi, ng, d_u, d_q, dx, courno ? d_c : nullptr, st));
+    CK(op_soa_to_aos(d_q, d_aos_q, np, 6, st));
+    CK(cudaMemcpyAsync(q, d_aos_q, sizeof(double) * 6 * np, cudaMemcpyDeviceToHost, st));
+    unsigned long long cb = 0;
+    if (courno) CK(cudaMemcpyAsync(&cb, d_c, sizeof cb, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (courno) {
+        double c;
+        memcpy(&c, &cb, sizeof c);
+        // cpu/ctoprim.cpp:69: courno = MAX(MAX(courmx, courmy), MAX(courmz, courno))
+        if (c > *courno) *courno = c;
+    }
+    return CNS_OK;
+}
+
+extern "C" int cns_hypterm(const int lo[3], const int hi[3], int ng, const double dx[3], const double* cons,
+                           const double* q, double* flux) {
+    int rc = check_bounds(lo, hi, ng);
+    if (rc) return rc;
+    if (!cons || !q || !flux || !dx) return fail(CNS_ERR_INVALID, "null array");
+    long long np = 1, ni = 1;
+    for (int a = 0; a < 3; a++) {
+        np *= (hi[a] - lo[a] + 1 + 2 * ng);
+        ni *= (hi[a] - lo[a] + 1);
+    }
+    const size_t need = sizeof(double) * (size_t)(np * 22 + ni * 10);
+    void* ws;
+    cudaStream_t st;
+    if ((rc = workspace(need, &ws, &st))) return rc;
+    double* a_c = (double*)ws;
+    double* a_q = a_c + 5 * np;
+    double* s_c = a_q + 6 * np;
+    double* s_q = s_c + 5 * np;
+    double* s_f = s_q + 6 * np;
+    double* a_f = s_f + 5 * ni;
+    CK(cudaMemcpyAsync(a_c, cons, sizeof(double) * 5 * np, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(a_q, q, sizeof(double) * 6 * np, cudaMemcpyHostToDevice, st));
+    CK(op_aos_to_soa(a_c, s_c, np, 5, st));
+    CK(op_aos_to_soa(a_q, s_q, np, 6, st));
+    CK(op_hypterm(lo, hi, ng, s_c, s_q, s_f, dx, st));
+    CK(op_soa_to_aos(s_f, a_f, ni, 5, st));
+    CK(cudaMemcpyAsync(flux, a_f, sizeof(double) * 5 * ni, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return CNS_OK;
+}
+
+extern "C" int cns_diffterm(const int lo[3], const int hi[3], int ng, const double dx[3], const double* q,
+                            double* difflux, double eta, double alam) {
+    int rc = check_bounds(lo, hi, ng);
+    if (rc) return rc;
+    if (!q || !difflux || !dx) return fail(CNS_ERR_INVALID, "null array");
+    long long np = 1, ni = 1;
+    for (int a = 0; a < 3; a++) {
+        np *= (hi[a] - lo[a] + 1 + 2 * ng);
+        ni *= (hi[a] - lo[a] + 1);
+    }
+    const size_t need = sizeof(double) * (size_t)(np * (6 + 6 + 9) + ni * 10);
+    void* ws;
+    cudaStream_t st;
+    if ((rc = workspace(need, &ws, &st))) return rc;
+    double* a_q = (double*)ws;
+    double* s_q = a_q + 6 * np;
+    double* tmp = s_q + 6 * np;
+    double* s_d = tmp + 9 * np;
+    double* a_d = s_d + 5 * ni;
+    CK(cudaMemcpyAsync(a_q, q, sizeof(double) * 6 * np, cudaMemcpyHostToDevice, st));
+    CK(op_aos_to_soa(a_q, s_q, np, 6, st));
+    CK(op_diffterm(lo, hi, ng, s_q, tmp, s_d, dx, eta, alam, st));
+    CK(op_soa_to_aos(s_d, a_d, ni, 5, st));
+    CK(cudaMemcpyAsync(difflux, a_d, sizeof(double) * 5 * ni, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return CNS_OK;
+}
+
+extern "C" int cns_fill_boundary(double* U, const int dim[3], const int dim_ng[3]) {
+    if (!U || !dim || !dim_ng) return fail(CNS_ERR_INVALID, "null argument");
+    for (int a = 0; a < 3; a++) {
+        if (dim[a] < CNS_NG) return fail(CNS_ERR_INVALID, "dim[%d]=%d < %d", a, dim[a], CNS_NG);
+        if (dim_ng[a] != dim[a] + 2 * CNS_NG) return fail(CNS_ERR_INVALID, "dim_ng[%d] != dim[%d]+8", a, a);
+    }
+    const long long np = (long long)dim_ng[0] * dim_ng[1] * dim_ng[2];
+    void* ws;
+    cudaStream_t st;
+    int rc = workspace(sizeof(double) * 5 * np, &ws, &st);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ws, U, sizeof(double) * 5 * np, cudaMemcpyHostToDevice, st));
+    CK(op_fill_ghosts_aos((double*)ws, dim, 5, st));
+    CK(cudaMemcpyAsync(U, ws, sizeof(double) * 5 * np, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return CNS_OK;
+}
+
+// A per-thread cache of one box for the host-array advance entry points, so that repeated
+// new_advance calls on the same problem reuse the device state allocation.
+struct BoxCache {
+    cns_box* box = nullptr;
+    ~BoxCache() {
+        if (box) cns_box_destroy(box);
+    }
+};
+static thread_local BoxCache g_cache;
+
+static bool same_desc(const cns_box_desc& a, const cns_box_desc& b) {
+    return memcmp(a.n, b.n, sizeof a.n) == 0 && memcmp(a.dx, b.dx, sizeof a.dx) == 0 && a.cfl == b.cfl &&
+           a.eta == b.eta && a.alam == b.alam && a.precision == b.precision;
+}
+
+static int cached_box(const cns_box_desc& d, cns_box** out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (g_cache.box && (g_cache.box->dev != dev || !same_desc(g_cache.box->desc, d))) {
+        cns_box_destroy(g_cache.box);
+        g_cache.box = nullptr;
+    }
+    if (!g_cache.box) {
+        int rc = cns_box_create(&d, &g_cache.box);
+        if (rc) return rc;
+    }
+    *out = g_cache.box;
+    return CNS_OK;
+}
+
+// Copy a host state in, fill its ghosts (the reference's fill_boundary at the start of the
+// step), run nsteps, and copy back the interior of the result with the ghosts of the last
+// step's start state -- what the reference leaves in U (cpu/advance.cpp:45,144-153).
+static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt_hist) {
+    cns_box* b;
+    int rc = cached_box(d, &b);
+    if (rc) return rc;
+    const size_t bytes = aos_bytes(b);
+    CK(cudaMemcpyAsync(b->d_aos, U, bytes, cudaMemcpyHostToDevice, b->stream));
+    if ((rc = cns_box_upload_device(b, b->d_aos))) return rc;
+    int done = 0;
+    while (done < nsteps) {
+        const int chunk = std::min(nsteps - done, DTLOG_CAP);
+        if (done + chunk == nsteps) {
+            // the last step's start state supplies the ghosts
+            if (chunk > 1 && (rc = cns_box_advance(b, chunk - 1))) return rc;
+            CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
+            if ((rc = cns_box_advance(b, 1))) return rc;
+        } else if ((rc = cns_box_advance(b, chunk))) {
+            return rc;
+        }
+        if (dt_hist) {
+            std::vector<double> log(DTLOG_CAP);
+            CK(cudaMemcpyAsync(log.data(), b->view.dtlog, sizeof(double) * DTLOG_CAP, cudaMemcpyDeviceToHost, b->stream));
+            CK(cudaStreamSynchronize(b->stream));
+            for (int s = 0; s < chunk; s++) dt_hist[done + s] = log[(done + s) & (DTLOG_CAP - 1)];
+        }
+        done += chunk;
+    }
+    if (nsteps == 0) CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
+    CK(op_box_to_aos(b->view, b->d_aos, 0, b->stream));
+    CK(cudaMemcpyAsync(U, b->d_aos, bytes, cudaMemcpyDeviceToHost, b->stream));
+    int health = 0;
+    rc = cns_box_sync(b, &health);
+    return rc;
+}
+
+extern "C" int cns_advance_host(double* U, const int n[3], const double dx[3], double cfl, double eta, double alam,
+                                int nsteps, int precision, double* dt_hist) {
+    if (!U || !n || !dx) return fail(CNS_ERR_INVALID, "null argument");
+    if (nsteps < 0) return fail(CNS_ERR_INVALID, "nsteps < 0");
+    cns_box_desc d;
+    memset(&d, 0, sizeof d);
+    for (int a = 0; a < 3; a++) {
+        d.n[a] = n[a];
+        d.dx[a] = dx[a];
+    }
+    d.cfl = cfl;
+    d.eta = eta;
+    d.alam = alam;
+    d.precision = precision;
+    int rc = validate_desc(&d);
+    if (rc) return rc;
+    return host_advance(d, U, nsteps, dt_hist);
+}
+
+extern "C" int cns_new_advance(const cns_global_const_t* h, double* U, double* Unew, double* Q, double* D, double* F,
+                               double* dt) {
+    (void)Unew, (void)Q, (void)D, (void)F;
+    if (!h || !U) return fail(CNS_ERR_INVALID, "null argument");
+    if (h->ng != CNS_NG || h->nc != CNS_NC)
+        return fail(CNS_ERR_INVALID, "ng=%d nc=%d: this build supports ng=%d, nc=%d", h->ng, h->nc, CNS_NG, CNS_NC);
+    double dt1 = 0.0;
+    int rc = cns_advance_host(U, h->dim, h->dx, h->cfl, h->eta, h->alam, 1, CNS_FP64, &dt1);
+    if (rc == CNS_OK && dt) *dt = dt1;
+    return rc;
+}

@@ -1,0 +1,121 @@
+// cns_common.cuh -- shared device definitions for the GB300 CNS_NoSpec RK3 advance.
+//
+// Device layout of one periodic box (n0 x n1 x n2 interior cells, NG = 4 ghost cells a side):
+// structure of arrays, one field after another; inside a field the reference's spatial order
+// (i slowest, k fastest, cpu/helper_functions.cpp:100-122) with each k row padded to `pk`
+// elements (a multiple of 32, so every row starts on a 128-byte boundary for FP32 and FP64).
+//   elem(f, i, j, k) = f*fs + i*si + j*sj + k      (i, j, k ghost-inclusive, 0..n+7)
+// i pairs with dx[0], j with dx[1], k with dx[2], exactly as in the reference.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CNS_NG 4
+#define CNS_NC 5
+
+namespace cns {
+
+// ---- physics and stencil constants (cpu/ctoprim.cpp:23-24, cpu/header.h:88-91,
+//      cpu/diffterm.cpp:48-52) -------------------------------------------------------------
+constexpr double kGamma = 1.4;
+constexpr double kGm1 = kGamma - 1.0;  // the reference forms (GAMMA-1.0) the same way
+constexpr double kCv = 8.3333333333e6;
+constexpr double kAlp = 0.8, kBet = -0.2, kGam = 4.0 / 105.0, kDel = -1.0 / 280.0;
+constexpr double kCenter = -205.0 / 72.0, kOff1 = 8.0 / 5.0, kOff2 = -0.2, kOff3 = 8.0 / 315.0,
+                 kOff4 = -1.0 / 560.0;
+
+// ---- field indices ----------------------------------------------------------------------
+// Conserved state (FP64 always): rho, rho u, rho v, rho w, rho E  (cpu/header.h:20-26).
+enum { URHO = 0, UMX, UMY, UMZ, UENE };
+// Primitive/flux set P (precision R): what the stencils read.  Each is produced once per
+// cell by the epilogue of the previous stage (ctoprim fused there) with its periodic ghost
+// images, so no stencil ever recomputes a neighbour's primitive.
+enum {
+    PU = 0, PV, PW, PT,        // velocities and temperature (diffterm)
+    PMX, PMY, PMZ,             // rho u, rho v, rho w  (density flux)
+    PFUU, PFVV, PFWW,          // rho u u + p, rho v v + p, rho w w + p
+    PFUV, PFUW, PFVW,          // rho u v, rho u w, rho v w
+    PHU, PHV, PHW,             // (rho E + p) u, (rho E + p) v, (rho E + p) w
+    NPF
+};
+// Derivative set S (precision R), made by the derivative pass.
+enum { SX = 0,   // v_y + w_z  (differenced along x for the mixed terms of the x momentum)
+       SY,       // u_x + w_z  (along y)
+       SZ,       // u_x + v_y  (along z)
+       SPHI,     // eta * viscous dissipation
+       NSF };
+
+// Per-box coefficient table, folded with 1/dx and the transport coefficients so that every
+// stencil tap is one fused multiply-add.  Kept in FP64 (plain form) and FP32 (mixed form).
+template <class R>
+struct CoefT {
+    R da[3][4];     // first derivative along d: a_m / dx_d
+    R ha[3][4];     // convective flux divergence: -a_m / dx_d
+    R mx[3][4];     // mixed viscous term: (eta/3) a_m / dx_d
+    R vl[3][3][4];  // viscous Laplacian of velocity c along d: eta (4/3 if c==d) b_m / dx_d^2
+    R vc[3];        // its centre weight: eta c0 sum_d (4/3 if c==d) / dx_d^2
+    R tl[3][4];     // heat conduction along d: alam b_m / dx_d^2
+    R tc;           // alam c0 sum_d 1/dx_d^2
+    R cour[3];      // 1/dx_d (Courant number)
+    R eta;          // viscosity
+};
+
+// Device scalars of one box (written by kernels only).
+struct BoxScalars {
+    unsigned long long courno_bits;  // running max of the Courant number (bits of a positive double)
+    double dt;                       // dt of the step in progress (or the next one, between steps)
+    double dt_last;                  // dt of the last completed step
+    int pbase;                       // which P set holds the primitives of the step's start state
+    int nsteps_done;
+    int status;                      // HEALTH_* bits, sticky
+    int pad;
+};
+
+constexpr int DTLOG_CAP = 1024;
+
+enum { HEALTH_OK = 0, HEALTH_NONPOS_RHO = 1, HEALTH_NONFINITE = 2, HEALTH_NONPOS_EINT = 4 };
+
+// Everything a kernel needs about one box.  Kept in device memory (one entry per box) so
+// that a batched launch can walk tiles of many boxes.
+struct BoxView {
+    int n[3];               // interior dims
+    int pk;                 // padded k row (elements)
+    long long sj, si, fs;   // strides (elements)
+    double* U;              // 5 fields, FP64: state at the start of the step
+    double* Us;             // 5 fields, FP64: stage state
+    void* P[2];             // NPF fields each, precision R
+    void* S;                // NSF fields, precision R
+    BoxScalars* sc;
+    double* dtlog;          // dt of completed steps, ring of DTLOG_CAP entries
+    double cfl;
+    int precision;          // 0 = plain FP64, 1 = mixed
+    int pad;
+    CoefT<double> c64;
+    CoefT<float> c32;
+};
+
+// A unit of work: one tile of one box.  Tiles are TI x TJ x TK cells with origin (i0,j0,k0).
+struct Tile {
+    int box, i0, j0, k0;
+};
+
+__host__ __device__ inline long long cell_off(const BoxView& b, int i, int j, int k) {
+    // (i, j, k) interior indices, 0-based; returns the element offset inside one field
+    return (long long)(i + CNS_NG) * b.si + (long long)(j + CNS_NG) * b.sj + (k + CNS_NG);
+}
+
+// Positive doubles order like their bit patterns; the Courant max uses integer atomics.
+__device__ inline unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+
+// Reciprocal for FP64: an FP32 seed refined by one third-order Newton-series step
+// r <- r (1 + e + e^2), e = 1 - x r (Householder's method of order 3 for 1/x).  The seed's
+// relative error e0 ~ 1e-7 becomes ~e0^3, so the result is within a few ulp of 1/x for
+// normal FP32-representable x (the densities here are ~1e-3).  Costs three FP64 FMAs
+// instead of a full IEEE division.
+__device__ inline double rcp_nr(double x) {
+    double r = (double)(1.0f / (float)x);
+    double e = fma(-x, r, 1.0);
+    return fma(r, fma(e, e, e), r);
+}
+
+}  // namespace cns

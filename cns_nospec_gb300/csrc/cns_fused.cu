@@ -1,0 +1,251 @@
+// cns_fused.cu -- persistent tile-walking kernels for the RK3 stages (see cns_fused.cuh).
+//
+// Every kernel walks a work list of tiles (box, i0, j0, k0); one launch covers every box of a
+// batch.  A tile is TI x TJ x TK cells (k = unit stride), one cell per thread.
+#include "cns_fused.cuh"
+#include "cns_internal.h"
+
+namespace cns {
+
+template <class R>
+__device__ __forceinline__ R ld(const R* p) { return __ldg(p); }
+
+// ---- k_prim: primitives + flux functions + Courant of the uploaded state -------------------
+template <class R, int TI, int TJ, int TK>
+__global__ void __launch_bounds__(TI* TJ* TK) k_prim(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
+                                                     int ntiles) {
+    const int tk = threadIdx.x % TK, tj = (threadIdx.x / TK) % TJ, ti = threadIdx.x / (TK * TJ);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const Tile T = tiles[t];
+        const BoxView& b = boxes[T.box];
+        const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
+        double cour = 0.0;
+        int health = 0;
+        if (i < b.n[0] && j < b.n[1] && k < b.n[2]) {
+            const long long c = cell_off(b, i, j, k);
+            double un[5];
+#pragma unroll
+            for (int l = 0; l < 5; l++) un[l] = b.U[c + l * b.fs];
+            R* Pw = (R*)b.P[b.sc->pbase];
+            cour = epilogue<R>(b, Pw, c, i, j, k, un, true, &health);
+        }
+        if (health) atomicOr(&b.sc->status, health);
+        courant_fold(b, cour);
+    }
+}
+
+// ---- k_deriv: first derivatives of (u,v,w) -> mixed-term sums and viscous dissipation -------
+template <class R, int TI, int TJ, int TK>
+__global__ void __launch_bounds__(TI* TJ* TK) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
+                                                      int ntiles, int stage) {
+    const int tk = threadIdx.x % TK, tj = (threadIdx.x / TK) % TJ, ti = threadIdx.x / (TK * TJ);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const Tile T = tiles[t];
+        const BoxView& b = boxes[T.box];
+        const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
+        if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+        const int pr = b.sc->pbase ^ ((stage - 1) & 1);
+        const R* P = (const R*)b.P[pr];
+        R* S = (R*)b.S;
+        const long long c = cell_off(b, i, j, k), fs = b.fs, si = b.si, sj = b.sj;
+        const CoefT<R>& cf = coefs<R>(b);
+        const R* pu = P + PU * fs + c;
+        const R* pv = P + PV * fs + c;
+        const R* pw = P + PW * fs + c;
+        // cpu/diffterm.cpp:73-151 (the nine first derivatives), at this cell only
+        const R ux = d1(pu, si, cf.da[0]), uy = d1(pu, sj, cf.da[1]), uz = d1(pu, 1, cf.da[2]);
+        const R vx = d1(pv, si, cf.da[0]), vy = d1(pv, sj, cf.da[1]), vz = d1(pv, 1, cf.da[2]);
+        const R wx = d1(pw, si, cf.da[0]), wy = d1(pw, sj, cf.da[1]), wz = d1(pw, 1, cf.da[2]);
+        // cpu/diffterm.cpp:294-304: viscous dissipation
+        const R divu = (R)(2.0 / 3.0) * (ux + vy + wz);
+        const R tauxx = fma((R)2, ux, -divu), tauyy = fma((R)2, vy, -divu), tauzz = fma((R)2, wz, -divu);
+        const R tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
+        R phi = tauxx * ux;
+        phi = fma(tauyy, vy, phi);
+        phi = fma(tauzz, wz, phi);
+        phi = fma(tauxy, tauxy, phi);
+        phi = fma(tauxz, tauxz, phi);
+        phi = fma(tauyz, tauyz, phi);
+        store_img(S + SX * fs, b, c, i, j, k, vy + wz, 1);
+        store_img(S + SY * fs, b, c, i, j, k, ux + wz, 2);
+        store_img(S + SZ * fs, b, c, i, j, k, ux + vy, 4);
+        S[SPHI * fs + c] = cf.eta * phi;
+    }
+}
+
+// ---- k_assemble: D + F, RK stage combine, fused ctoprim/flux/ghost write-back -------------
+template <class R, int STAGE, int TI, int TJ, int TK>
+__global__ void __launch_bounds__(TI* TJ* TK) k_assemble(const BoxView* __restrict__ boxes,
+                                                         const Tile* __restrict__ tiles, int ntiles) {
+    const int tk = threadIdx.x % TK, tj = (threadIdx.x / TK) % TJ, ti = threadIdx.x / (TK * TJ);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const Tile T = tiles[t];
+        const BoxView& b = boxes[T.box];
+        const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
+        double cour = 0.0;
+        int health = 0;
+        if (i < b.n[0] && j < b.n[1] && k < b.n[2]) {
+            const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
+            const R* Pr = (const R*)b.P[pr];
+            R* Pw = (R*)b.P[pr ^ 1];
+            const R* S = (const R*)b.S;
+            const long long c = cell_off(b, i, j, k), fs = b.fs, si = b.si, sj = b.sj;
+            const CoefT<R>& cf = coefs<R>(b);
+            const R* pu = Pr + PU * fs + c;
+            const R* pv = Pr + PV * fs + c;
+            const R* pw = Pr + PW * fs + c;
+            const R* pt = Pr + PT * fs + c;
+            const R u0 = ld(pu), v0 = ld(pv), w0 = ld(pw), t0 = ld(pt);
+            // diffterm momentum components (cpu/diffterm.cpp:155-269)
+            R dmx = cf.vc[0] * u0;
+            dmx = d2acc(dmx, pu, si, cf.vl[0][0]);
+            dmx = d2acc(dmx, pu, sj, cf.vl[0][1]);
+            dmx = d2acc(dmx, pu, 1, cf.vl[0][2]);
+            dmx = d1acc(dmx, S + SX * fs + c, si, cf.mx[0]);
+            R dmy = cf.vc[1] * v0;
+            dmy = d2acc(dmy, pv, si, cf.vl[1][0]);
+            dmy = d2acc(dmy, pv, sj, cf.vl[1][1]);
+            dmy = d2acc(dmy, pv, 1, cf.vl[1][2]);
+            dmy = d1acc(dmy, S + SY * fs + c, sj, cf.mx[1]);
+            R dmz = cf.vc[2] * w0;
+            dmz = d2acc(dmz, pw, si, cf.vl[2][0]);
+            dmz = d2acc(dmz, pw, sj, cf.vl[2][1]);
+            dmz = d2acc(dmz, pw, 1, cf.vl[2][2]);
+            dmz = d1acc(dmz, S + SZ * fs + c, 1, cf.mx[2]);
+            // diffterm energy component (cpu/diffterm.cpp:272-311)
+            R de = fma(cf.tc, t0, ld(S + SPHI * fs + c));
+            de = d2acc(de, pt, si, cf.tl[0]);
+            de = d2acc(de, pt, sj, cf.tl[1]);
+            de = d2acc(de, pt, 1, cf.tl[2]);
+            de = fma(dmx, u0, de);
+            de = fma(dmy, v0, de);
+            de = fma(dmz, w0, de);
+            // hypterm (cpu/hypterm.cpp:29-208), added to D
+            R f[5];
+            f[0] = d1(Pr + PMX * fs + c, si, cf.ha[0]);
+            f[0] = d1acc(f[0], Pr + PMY * fs + c, sj, cf.ha[1]);
+            f[0] = d1acc(f[0], Pr + PMZ * fs + c, 1, cf.ha[2]);
+            f[1] = d1acc(dmx, Pr + PFUU * fs + c, si, cf.ha[0]);
+            f[1] = d1acc(f[1], Pr + PFUV * fs + c, sj, cf.ha[1]);
+            f[1] = d1acc(f[1], Pr + PFUW * fs + c, 1, cf.ha[2]);
+            f[2] = d1acc(dmy, Pr + PFUV * fs + c, si, cf.ha[0]);
+            f[2] = d1acc(f[2], Pr + PFVV * fs + c, sj, cf.ha[1]);
+            f[2] = d1acc(f[2], Pr + PFVW * fs + c, 1, cf.ha[2]);
+            f[3] = d1acc(dmz, Pr + PFUW * fs + c, si, cf.ha[0]);
+            f[3] = d1acc(f[3], Pr + PFVW * fs + c, sj, cf.ha[1]);
+            f[3] = d1acc(f[3], Pr + PFWW * fs + c, 1, cf.ha[2]);
+            f[4] = d1acc(de, Pr + PHU * fs + c, si, cf.ha[0]);
+            f[4] = d1acc(f[4], Pr + PHV * fs + c, sj, cf.ha[1]);
+            f[4] = d1acc(f[4], Pr + PHW * fs + c, 1, cf.ha[2]);
+            // RK3 stage combine in FP64 (cpu/advance.cpp:78-85, 110-119, 144-153)
+            const double dt = b.sc->dt;
+            double un[5];
+#pragma unroll
+            for (int l = 0; l < 5; l++) {
+                const long long e = c + l * fs;
+                const double r = (double)f[l];
+                if (STAGE == 1) {
+                    un[l] = fma(dt, r, b.U[e]);
+                    b.Us[e] = un[l];
+                } else if (STAGE == 2) {
+                    un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                    b.Us[e] = un[l];
+                } else {
+                    un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
+                    b.U[e] = un[l];
+                }
+            }
+            cour = epilogue<R>(b, Pw, c, i, j, k, un, STAGE == 3, &health);
+        }
+        if (health) atomicOr(&b.sc->status, health);
+        if (STAGE == 3) courant_fold(b, cour);
+    }
+}
+
+// ---- k_stepend: dt for the next step from the Courant max (cpu/advance.cpp:52-58) ----------
+__global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int flip) {
+    const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bx >= nboxes) return;
+    BoxScalars* s = boxes[bx].sc;
+    double courno = __longlong_as_double((long long)s->courno_bits);
+    courno = (courno > 1.0e-50) ? courno : 1.0e-50;
+    if (flip) {
+        boxes[bx].dtlog[s->nsteps_done & (DTLOG_CAP - 1)] = s->dt;
+        s->dt_last = s->dt;
+        s->pbase ^= 1;
+        s->nsteps_done += 1;
+    }
+    s->dt = boxes[bx].cfl / courno;
+    s->courno_bits = 0ull;
+}
+
+// ---- launch helpers ---------------------------------------------------------------------
+constexpr int TI = 2, TJ = 4, TK = 32, NT = TI * TJ * TK;
+
+static int grid_for(const void* fn, int ntiles) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, NT, 0);
+    if (per < 1) per = 1;
+    int g = nsm * per;
+    return ntiles < g ? ntiles : g;
+}
+
+void tile_shape(int* ti, int* tj, int* tk) {
+    *ti = TI;
+    *tj = TJ;
+    *tk = TK;
+}
+
+template <class R>
+static cudaError_t launch_prim_t(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
+    auto fn = k_prim<R, TI, TJ, TK>;
+    fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+    return cudaGetLastError();
+}
+template <class R>
+static cudaError_t launch_deriv_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    auto fn = k_deriv<R, TI, TJ, TK>;
+    fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles, stage);
+    return cudaGetLastError();
+}
+template <class R>
+static cudaError_t launch_assemble_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    if (stage == 1) {
+        auto fn = k_assemble<R, 1, TI, TJ, TK>;
+        fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+    } else if (stage == 2) {
+        auto fn = k_assemble<R, 2, TI, TJ, TK>;
+        fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+    } else {
+        auto fn = k_assemble<R, 3, TI, TJ, TK>;
+        fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    return precision ? launch_prim_t<float>(boxes, tiles, ntiles, st) : launch_prim_t<double>(boxes, tiles, ntiles, st);
+}
+cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
+                         cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    return precision ? launch_deriv_t<float>(boxes, tiles, ntiles, stage, st)
+                     : launch_deriv_t<double>(boxes, tiles, ntiles, stage, st);
+}
+cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
+                            cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    return precision ? launch_assemble_t<float>(boxes, tiles, ntiles, stage, st)
+                     : launch_assemble_t<double>(boxes, tiles, ntiles, stage, st);
+}
+cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st) {
+    if (nboxes <= 0) return cudaSuccess;
+    k_stepend<<<(nboxes + 127) / 128, 128, 0, st>>>(boxes, nboxes, flip);
+    return cudaGetLastError();
+}
+
+}  // namespace cns

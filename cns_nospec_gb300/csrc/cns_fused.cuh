@@ -1,0 +1,199 @@
+// cns_fused.cuh -- the fused RK3 stage kernels (plain FP64 and mixed FP32/FP64).
+//
+// One RK3 step of the reference (new_advance, cpu/advance.cpp:13-154) is, per box:
+//
+//   k_prim       (once, after an upload)  ctoprim + flux functions of U -> P[pbase], Courant
+//   k_stepend    dt = cfl / max(courno, 1e-50)          (cpu/advance.cpp:52-58)
+//   stage s = 1, 2, 3:
+//     k_deriv     first derivatives of (u,v,w) -> S = (v_y+w_z, u_x+w_z, u_x+v_y, eta*Phi)
+//     k_assemble  diffterm + hypterm from P and S, RK stage combine in FP64
+//                 (cpu/advance.cpp:78-85, 110-119, 144-153), then, fused into the
+//                 write-back, ctoprim + flux functions of the new stage state -> the other P
+//                 set with its periodic ghost images (fill_boundary fused,
+//                 cpu/helper_functions.cpp:226-262); stage 3 also folds the Courant number
+//                 of U^{n+1} (cpu/ctoprim.cpp:50-69) into the box's running max.
+//   k_stepend    flip the P set, next dt.
+//
+// GB300's FP64 rate is 1/67 of its FP32 rate, so the plain form is bound by the FP64 pipe,
+// not by HBM: the kernels are arranged so that every FP64 quantity is computed exactly once
+// per cell (no halo recomputation of primitives or derivatives) and every stencil tap is one
+// FMA with a coefficient pre-folded with 1/dx, eta or alam.
+//
+// Algebraic regrouping against the reference (same discrete operators; rounding differs at
+// the level of a few ulp):
+//   * hypterm's products cons*u at each neighbour become per-cell flux functions
+//     (rho u u + p, rho u v, ..., (rho E + p) u) differenced by the same 8-point stencil
+//     (cpu/hypterm.cpp:43-204);
+//   * diffterm's vyx + wzx, uxy + wzy, uxz + vyz become one stencil each on the per-cell sums
+//     v_y + w_z, u_x + w_z, u_x + v_y (cpu/diffterm.cpp:177-265);
+//   * the three second differences of each Laplacian share one centre tap.
+#pragma once
+#include "cns_common.cuh"
+
+namespace cns {
+
+template <class R>
+__device__ __forceinline__ const CoefT<R>& coefs(const BoxView& b);
+template <>
+__device__ __forceinline__ const CoefT<double>& coefs<double>(const BoxView& b) { return b.c64; }
+template <>
+__device__ __forceinline__ const CoefT<float>& coefs<float>(const BoxView& b) { return b.c32; }
+
+// acc + sum_m a_m (p[m s] - p[-m s])
+template <class R>
+__device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, const R* a) {
+    acc = fma(a[0], __ldg(p + s) - __ldg(p - s), acc);
+    acc = fma(a[1], __ldg(p + 2 * s) - __ldg(p - 2 * s), acc);
+    acc = fma(a[2], __ldg(p + 3 * s) - __ldg(p - 3 * s), acc);
+    acc = fma(a[3], __ldg(p + 4 * s) - __ldg(p - 4 * s), acc);
+    return acc;
+}
+template <class R>
+__device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a) {
+    R acc = a[0] * (__ldg(p + s) - __ldg(p - s));
+    acc = fma(a[1], __ldg(p + 2 * s) - __ldg(p - 2 * s), acc);
+    acc = fma(a[2], __ldg(p + 3 * s) - __ldg(p - 3 * s), acc);
+    acc = fma(a[3], __ldg(p + 4 * s) - __ldg(p - 4 * s), acc);
+    return acc;
+}
+// acc + sum_m b_m (p[m s] + p[-m s])
+template <class R>
+__device__ __forceinline__ R d2acc(R acc, const R* __restrict__ p, long long s, const R* b) {
+    acc = fma(b[0], __ldg(p + s) + __ldg(p - s), acc);
+    acc = fma(b[1], __ldg(p + 2 * s) + __ldg(p - 2 * s), acc);
+    acc = fma(b[2], __ldg(p + 3 * s) + __ldg(p - 3 * s), acc);
+    acc = fma(b[3], __ldg(p + 4 * s) + __ldg(p - 4 * s), acc);
+    return acc;
+}
+
+// Store a value and its periodic face images along the axes in `mask` (1 = i, 2 = j, 4 = k).
+template <class R>
+__device__ __forceinline__ void store_img(R* __restrict__ f, const BoxView& b, long long c, int i, int j, int k,
+                                          R v, int mask) {
+    f[c] = v;
+    if (mask & 1) {
+        if (i < CNS_NG) f[c + (long long)b.n[0] * b.si] = v;
+        if (i >= b.n[0] - CNS_NG) f[c - (long long)b.n[0] * b.si] = v;
+    }
+    if (mask & 2) {
+        if (j < CNS_NG) f[c + (long long)b.n[1] * b.sj] = v;
+        if (j >= b.n[1] - CNS_NG) f[c - (long long)b.n[1] * b.sj] = v;
+    }
+    if (mask & 4) {
+        if (k < CNS_NG) f[c + b.n[2]] = v;
+        if (k >= b.n[2] - CNS_NG) f[c - b.n[2]] = v;
+    }
+}
+
+// Health bits from raw IEEE fields (integer ops only; no FP64 pipe work).
+__device__ __forceinline__ int health_bits(double rho, double eint) {
+    unsigned long long rb = dbits(rho), eb = dbits(eint);
+    int h = 0;
+    if ((rb >> 63) || rb == 0ull) h |= HEALTH_NONPOS_RHO;
+    if (((rb >> 52) & 0x7FF) == 0x7FF || ((eb >> 52) & 0x7FF) == 0x7FF) h |= HEALTH_NONFINITE;
+    if ((eb >> 63) || eb == 0ull) h |= HEALTH_NONPOS_EINT;
+    return h;
+}
+
+// ctoprim + flux functions of one cell's FP64 conserved state, written to the P set `Pw`
+// with the periodic face images each field's stencils need.  Returns the cell's Courant
+// number (only formed when `want_cour`).  Plain form: everything in FP64 (reciprocal by
+// rcp_nr).  Mixed form: E/rho and the subtraction e = E/rho - |u|^2/2 in FP64, the rest in
+// FP32.
+template <class R>
+__device__ __forceinline__ double epilogue(const BoxView& b, R* __restrict__ Pw, long long c, int i, int j, int k,
+                                           const double un[5], bool want_cour, int* health);
+
+template <>
+__device__ __forceinline__ double epilogue<double>(const BoxView& b, double* __restrict__ Pw, long long c, int i,
+                                                   int j, int k, const double un[5], bool want_cour, int* health) {
+    const long long fs = b.fs;
+    const double rho = un[0], mx = un[1], my = un[2], mz = un[3], E = un[4];
+    const double rinv = rcp_nr(rho);
+    const double u = mx * rinv, v = my * rinv, w = mz * rinv;
+    const double ke = fma(u, u, fma(v, v, w * w));
+    const double eint = fma(-0.5, ke, E * rinv);
+    const double p = (kGm1 * eint) * rho;
+    const double T = eint * (1.0 / kCv);
+    const double H = E + p;
+    *health |= health_bits(rho, eint);
+    store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
+    store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
+    store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
+    store_img(Pw + PT * fs, b, c, i, j, k, T, 7);
+    store_img(Pw + PMX * fs, b, c, i, j, k, mx, 1);
+    store_img(Pw + PMY * fs, b, c, i, j, k, my, 2);
+    store_img(Pw + PMZ * fs, b, c, i, j, k, mz, 4);
+    store_img(Pw + PFUU * fs, b, c, i, j, k, fma(mx, u, p), 1);
+    store_img(Pw + PFVV * fs, b, c, i, j, k, fma(my, v, p), 2);
+    store_img(Pw + PFWW * fs, b, c, i, j, k, fma(mz, w, p), 4);
+    store_img(Pw + PFUV * fs, b, c, i, j, k, mx * v, 3);
+    store_img(Pw + PFUW * fs, b, c, i, j, k, mx * w, 5);
+    store_img(Pw + PFVW * fs, b, c, i, j, k, my * w, 6);
+    store_img(Pw + PHU * fs, b, c, i, j, k, H * u, 1);
+    store_img(Pw + PHV * fs, b, c, i, j, k, H * v, 2);
+    store_img(Pw + PHW * fs, b, c, i, j, k, H * w, 4);
+    if (!want_cour) return 0.0;
+    const double cs = sqrt((kGamma * p) * rinv);
+    const double cx = (cs + fabs(u)) * b.c64.cour[0];
+    const double cy = (cs + fabs(v)) * b.c64.cour[1];
+    const double cz = (cs + fabs(w)) * b.c64.cour[2];
+    return fmax(fmax(cx, cy), cz);
+}
+
+template <>
+__device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __restrict__ Pw, long long c, int i,
+                                                  int j, int k, const double un[5], bool want_cour, int* health) {
+    const long long fs = b.fs;
+    const double rho = un[0], E = un[4];
+    const float rhof = (float)rho;
+    const float rf = 1.0f / rhof;
+    const float mx = (float)un[1], my = (float)un[2], mz = (float)un[3];
+    const float u = mx * rf, v = my * rf, w = mz * rf;
+    // E/rho to ~1e-15 in FP64 from the FP32 reciprocal: y0 = E r, y = y0 + (E - rho y0) r
+    const double r64 = (double)rf;
+    const double y0 = E * r64;
+    const double erho = fma(fma(-rho, y0, E), r64, y0);
+    const float ke = fmaf(u, u, fmaf(v, v, w * w));
+    const double eint = fma(-0.5, (double)ke, erho);  // the cancelling subtraction, in FP64
+    const float ef = (float)eint;
+    const float p = ((float)kGm1 * ef) * rhof;
+    const float T = ef * (float)(1.0 / kCv);
+    const float H = (float)E + p;
+    *health |= health_bits(rho, eint);
+    store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
+    store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
+    store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
+    store_img(Pw + PT * fs, b, c, i, j, k, T, 7);
+    store_img(Pw + PMX * fs, b, c, i, j, k, mx, 1);
+    store_img(Pw + PMY * fs, b, c, i, j, k, my, 2);
+    store_img(Pw + PMZ * fs, b, c, i, j, k, mz, 4);
+    store_img(Pw + PFUU * fs, b, c, i, j, k, fmaf(mx, u, p), 1);
+    store_img(Pw + PFVV * fs, b, c, i, j, k, fmaf(my, v, p), 2);
+    store_img(Pw + PFWW * fs, b, c, i, j, k, fmaf(mz, w, p), 4);
+    store_img(Pw + PFUV * fs, b, c, i, j, k, mx * v, 3);
+    store_img(Pw + PFUW * fs, b, c, i, j, k, mx * w, 5);
+    store_img(Pw + PFVW * fs, b, c, i, j, k, my * w, 6);
+    store_img(Pw + PHU * fs, b, c, i, j, k, H * u, 1);
+    store_img(Pw + PHV * fs, b, c, i, j, k, H * v, 2);
+    store_img(Pw + PHW * fs, b, c, i, j, k, H * w, 4);
+    if (!want_cour) return 0.0;
+    const float cs = sqrtf(((float)kGamma * p) * rf);
+    const float cx = (cs + fabsf(u)) * b.c32.cour[0];
+    const float cy = (cs + fabsf(v)) * b.c32.cour[1];
+    const float cz = (cs + fabsf(w)) * b.c32.cour[2];
+    return (double)fmaxf(fmaxf(cx, cy), cz);
+}
+
+// Warp max of positive doubles via their bit patterns; lane 0 folds it into the box max.
+__device__ __forceinline__ void courant_fold(const BoxView& b, double cour) {
+    unsigned long long v = dbits(cour);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (w > v) ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(&b.sc->courno_bits, v);
+}
+
+}  // namespace cns

@@ -1,0 +1,31 @@
+// cns_internal.h -- launchers shared between the kernel files and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include "cns_common.cuh"
+
+namespace cns {
+
+// fused RK3 stage kernels (cns_fused.cu); precision 0 = FP64 stencils, 1 = FP32 stencils
+void tile_shape(int* ti, int* tj, int* tk);
+cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st);
+cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
+                         cudaStream_t st);
+cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
+                            cudaStream_t st);
+cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st);
+
+// operator-level kernels and layout conversions (cns_ops.cu)
+cudaError_t op_aos_to_soa(const double* aos, double* soa, long long npts, int nc, cudaStream_t st);
+cudaError_t op_soa_to_aos(const double* soa, double* aos, long long npts, int nc, cudaStream_t st);
+cudaError_t op_ctoprim(const int lo[3], const int hi[3], int ng, const double* u, double* q, const double dx[3],
+                       unsigned long long* courno_bits, cudaStream_t st);
+cudaError_t op_hypterm(const int lo[3], const int hi[3], int ng, const double* cons, const double* q, double* flux,
+                       const double dx[3], cudaStream_t st);
+cudaError_t op_diffterm(const int lo[3], const int hi[3], int ng, const double* q, double* tmp9, double* difflux,
+                        const double dx[3], double eta, double alam, cudaStream_t st);
+cudaError_t op_fill_ghosts_aos(double* aos, const int n[3], int nc, cudaStream_t st);
+cudaError_t op_aos_to_box(const double* aos, const BoxView& b, cudaStream_t st);
+cudaError_t op_box_to_aos(const BoxView& b, double* aos, int ghosts, cudaStream_t st);
+cudaError_t probe_fp64(double* tflops);
+
+}  // namespace cns

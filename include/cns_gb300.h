@@ -1,0 +1,158 @@
+/*
+ * cns_gb300.h -- C ABI of the GB300-native CNS_NoSpec RK3 advance (libcns_gb300.so).
+ *
+ * The library replaces the reference's cpu/ hot path: new_advance and the operators it calls
+ * (cpu/advance.cpp:13-154, cpu/ctoprim.cpp:11-105, cpu/hypterm.cpp:11-209,
+ * cpu/diffterm.cpp:22-320, cpu/helper_functions.cpp:226-262).  Every entry point is plain C:
+ * pointers and sizes, no C++ or torch types.  All return an int status (cns_status); on
+ * failure cns_last_error() describes the cause.  Nothing here calls exit().
+ *
+ * Array layout at this boundary is the reference's host layout (allocate_4D,
+ * cpu/helper_functions.cpp:100-122): one contiguous block of doubles indexed
+ * [i][j][k][l], component l fastest, then k, then j, then i; i pairs with dx[0].
+ * Ghost-inclusive arrays (U, Q) have n+2*ng cells per axis; D/F are interior-only.
+ * A caller holding the reference's double**** trees passes &X[0][0][0][0].
+ *
+ * Threading: calls on different cns_box / cns_batch handles may run concurrently from
+ * different host threads; one handle must not be used by two threads at once.  The
+ * operator-level calls (cns_ctoprim, ...) share a per-thread device workspace.
+ */
+#ifndef CNS_GB300_H
+#define CNS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CNS_NG 4 /* ghost cells per side, cpu/header.h:16 */
+#define CNS_NC 5 /* conserved components, cpu/header.h:15 */
+
+typedef enum cns_status {
+    CNS_OK = 0,
+    CNS_ERR_INVALID = 1,   /* bad argument (sizes, ng, null pointer, ...) */
+    CNS_ERR_NOMEM = 2,     /* device or host allocation failed */
+    CNS_ERR_NONFINITE = 3, /* the state developed rho <= 0, e <= 0 or a non-finite value */
+    CNS_ERR_CUDA = 4,      /* a CUDA runtime call failed */
+    CNS_ERR_CAPACITY = 5,  /* a size above a documented maximum */
+    CNS_ERR_NODEVICE = 6   /* no CUDA device */
+} cns_status;
+
+typedef enum cns_precision {
+    CNS_FP64 = 0, /* plain form: FP64 throughout */
+    CNS_MIXED = 1 /* FP32 primitives/stencils/fluxes; FP64 e = E/rho - |u|^2/2 and RK3 state */
+} cns_precision;
+
+/* Layout-compatible with the reference's parameter struct global_const_t
+ * (cpu/header.h:47-86), so a caller can pass &h_const directly.  Only ng, nc, dim, dx, cfl,
+ * eta and alam are read; MAX_TEMP is 27 (cpu/header.h:36-45). */
+typedef struct cns_global_const {
+    int ng, nc, ncells;
+    int lo[3], hi[3], dim[3], dim_g[3];
+    int comp_offset_g, comp_offset, plane_offset_g, plane_offset;
+    int nsteps;
+    double dt;
+    double dx[3], dxinv[3];
+    double cfl, eta, alam;
+    double *temp[27];
+    double ALP, BET, GAM, DEL;
+    double OneThird, TwoThirds, FourThirds, OneQuarter, ThreeQuarters;
+    double CENTER, OFF1, OFF2, OFF3, OFF4;
+} cns_global_const_t;
+
+/* ---- library --------------------------------------------------------------------------- */
+const char *cns_last_error(void);          /* message of this thread's last failure */
+int cns_version(void);                     /* 100 * major + minor */
+int cns_set_device(int device);            /* select the CUDA device for this host thread */
+int cns_device_synchronize(void);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (a ~0.1 s probe kernel):
+ * the roofline denominator of the FP64-bound stencil kernels. */
+int cns_measure_fp64_peak(double *tflops);
+
+/* ---- operator level: the reference's per-operator surface, host arrays ---------------- */
+
+/* cpu/ctoprim.cpp:11-70 and 72-105 (header.h:99-115).  q over the ghost-inclusive box from u;
+ * when courno != NULL, *courno = max(*courno, max over interior of (c+|u_d|)/dx_d), exactly
+ * as the reference's courno argument.  lo/hi are ghost-offset interior bounds (lo = ng). */
+int cns_ctoprim(const int lo[3], const int hi[3], const double *u, double *q, const double dx[3], int ng,
+                double *courno);
+
+/* cpu/hypterm.cpp:11-209 (header.h:118-126).  flux is interior-indexed [n0][n1][n2][5]. */
+int cns_hypterm(const int lo[3], const int hi[3], int ng, const double dx[3], const double *cons,
+                const double *q, double *flux);
+
+/* cpu/diffterm.cpp:22-320 (header.h:129-138).  difflux is interior-indexed [n0][n1][n2][5]. */
+int cns_diffterm(const int lo[3], const int hi[3], int ng, const double dx[3], const double *q,
+                 double *difflux, double eta, double alam);
+
+/* cpu/helper_functions.cpp:226-262 (helper_functions.h:172-176): periodic ghost fill of a
+ * ghost-inclusive [dim+8]^3 x 5 block, in place. */
+int cns_fill_boundary(double *U, const int dim[3], const int dim_ng[3]);
+
+/* cpu/advance.cpp:13-154 (header.h:149-156): one RK3 step of U in place, dt out.
+ * Parameters come from *h (the reference's h_const).  Per-axis dims are honoured (the
+ * reference handles cubic boxes only).  As in the reference, U's ghost cells come back
+ * holding the periodic fill made at the start of the step.  Unew, Q, D and F are accepted
+ * for signature compatibility and are not touched (the device keeps its own state); they
+ * may be NULL.  Each call copies U in and out; cns_box_* keeps the state resident. */
+int cns_new_advance(const cns_global_const_t *h, double *U, double *Unew, double *Q, double *D, double *F,
+                    double *dt);
+
+/* nsteps RK3 steps of a host U (ghost-inclusive [n+8]^3 x 5) with one copy in and one out.
+ * dt_hist (nullable) receives each step's dt.  precision: cns_precision. */
+int cns_advance_host(double *U, const int n[3], const double dx[3], double cfl, double eta, double alam,
+                     int nsteps, int precision, double *dt_hist);
+
+/* ---- device-resident boxes ------------------------------------------------------------- */
+typedef struct cns_box cns_box;
+
+typedef struct cns_box_desc {
+    int n[3];       /* interior cells per axis, each >= 4 */
+    double dx[3];   /* cell sizes */
+    double cfl, eta, alam;
+    int precision;  /* cns_precision */
+} cns_box_desc;
+
+/* bytes of device memory one box of this description holds */
+long long cns_box_bytes(const cns_box_desc *desc);
+int cns_box_create(const cns_box_desc *desc, cns_box **out);
+int cns_box_destroy(cns_box *box);
+/* Run the box's work on `stream` (a cudaStream_t; NULL = the box's own stream). */
+int cns_box_set_stream(cns_box *box, void *stream);
+/* Copy a host ghost-inclusive AoS state in (ghost cells are ignored) / out (ghost cells get
+ * the periodic images of the interior).  Both block until the copy is done. */
+int cns_box_upload(cns_box *box, const double *U_host);
+int cns_box_download(cns_box *box, double *U_host);
+/* Same, from/to a device AoS buffer, asynchronously on the box's stream. */
+int cns_box_upload_device(cns_box *box, const double *U_dev);
+int cns_box_download_device(cns_box *box, double *U_dev);
+/* nsteps RK3 steps, asynchronous on the box's stream (replays a captured one-step graph). */
+int cns_box_advance(cns_box *box, int nsteps);
+/* Same, without graphs, with a CUDA event around every kernel launch; fills
+ * kernel_ms[CNS_KERN_COUNT] (summed device ms per kernel kind), kernel_launches[...] and
+ * *total_ms (first to last event).  Blocks until done. */
+enum { CNS_KERN_DERIV = 0, CNS_KERN_ASSEMBLE = 1, CNS_KERN_STEPEND = 2, CNS_KERN_PRIM = 3, CNS_KERN_COUNT = 4 };
+int cns_box_advance_timed(cns_box *box, int nsteps, double *kernel_ms, int *kernel_launches, double *total_ms);
+/* Blocks until the box's queued work is done; returns CNS_ERR_NONFINITE if the state
+ * went bad (then *health_bits, if given, says how). */
+int cns_box_sync(cns_box *box, int *health_bits);
+int cns_box_last_dt(cns_box *box, double *dt, int *nsteps_done);
+/* Kernel launches one cns_box_advance step issues (for launch accounting). */
+int cns_box_launches_per_step(const cns_box *box);
+
+/* ---- batches: many boxes advanced together, one launch per kernel and stage ------------ */
+typedef struct cns_batch cns_batch;
+int cns_batch_create(cns_batch **out);
+int cns_batch_destroy(cns_batch *batch);
+int cns_batch_set_stream(cns_batch *batch, void *stream);
+int cns_batch_add(cns_batch *batch, cns_box *box);
+int cns_batch_remove(cns_batch *batch, cns_box *box);
+int cns_batch_size(const cns_batch *batch);
+/* nsteps RK3 steps of every member (each with its own dt), replaying a captured graph of
+ * one step (rebuilt when membership changes).  Asynchronous. */
+int cns_batch_advance(cns_batch *batch, int nsteps);
+int cns_batch_sync(cns_batch *batch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CNS_GB300_H */

@@ -1,0 +1,102 @@
+"""Batched advance (many boxes per launch, graph-replayed) and the mixed-precision form."""
+import numpy as np
+import pytest
+
+from conftest import FP64_TOL, MIXED_TOL, normwise
+from cns_nospec_gb300 import initdata as I
+
+pytestmark = pytest.mark.gpu
+
+
+def _boxes(cns, specs):
+    out = []
+    for n, prec, amp, eta_f, seed in specs:
+        dx = I.box_dx(n)
+        U0 = I.initial_state(n, amp=amp, perturb=1e-3, seed=seed)
+        b = cns.Box(n, dx, I.CFL, I.ETA * eta_f, I.ALAM * eta_f, precision=prec)
+        b.upload(U0)
+        out.append((b, U0, n, prec, eta_f))
+    return out
+
+
+SPECS = [((16, 24, 20), 0, (1.0, 0.9, 1.1), 1.0, 1), ((33, 17, 40), 1, (0.8, 1.2, 1.0), 0.9, 2),
+         ((20, 20, 20), 0, (1.1, 1.1, 0.85), 1.15, 3), ((48, 16, 17), 1, (1.0, 1.0, 1.0), 1.05, 4),
+         ((9, 40, 12), 0, (0.95, 1.05, 1.2), 0.8, 5)]
+
+
+def test_batch_equals_alone_bitwise(gpu, cns):
+    """Every box's result in the mix is bit-identical to the same box advanced alone."""
+    mix = _boxes(cns, SPECS)
+    batch = cns.Batch()
+    for b, *_ in mix:
+        batch.add(b)
+    batch.advance(5)
+    batch.sync()
+    alone = _boxes(cns, SPECS)
+    for (bm, U0, n, prec, _), (ba, *_rest) in zip(mix, alone):
+        ba.advance(5)
+        A = ba.download()
+        M = bm.download()
+        assert np.array_equal(A, M), n
+    batch.close()
+
+
+def test_continuous_batching_join_and_leave(gpu, cns):
+    """Boxes that join or leave between steps still match their solo runs bit for bit."""
+    mix = _boxes(cns, SPECS[:3])
+    batch = cns.Batch()
+    batch.add(mix[0][0])
+    batch.add(mix[1][0])
+    batch.advance(2)            # boxes 0, 1: 2 steps
+    batch.add(mix[2][0])        # box 2 joins
+    batch.advance(3)            # boxes 0, 1: 5 steps; box 2: 3
+    batch.remove(mix[0][0])     # box 0 leaves at 5 steps
+    batch.advance(1)            # box 1: 6; box 2: 4
+    batch.sync()
+    expect = [5, 6, 4]
+    alone = _boxes(cns, SPECS[:3])
+    for (bm, *_), (ba, *_r), k in zip(mix, alone, expect):
+        ba.advance(k)
+        assert np.array_equal(ba.download(), bm.download())
+        assert bm.last_dt()[1] == k
+    batch.close()
+
+
+def test_batch_fp64_members_match_oracle(gpu, cns, oracle):
+    mix = _boxes(cns, [s for s in SPECS if s[1] == 0])
+    batch = cns.Batch()
+    for b, *_ in mix:
+        batch.add(b)
+    batch.advance(3)
+    batch.sync()
+    for b, U0, n, prec, f in mix:
+        ref, _ = oracle.advance(U0, 3, I.box_dx(n), I.CFL, I.ETA * f, I.ALAM * f)
+        assert normwise(b.download(), ref).max() <= FP64_TOL
+    batch.close()
+
+
+def test_mixed_32cube_10_steps_vs_oracle(gpu, cns, oracle):
+    n = 32
+    U0 = I.initial_state(n)
+    ref, rdt = oracle.advance(U0, 10, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    U = U0.copy()
+    dts = cns.advance_host(U, 10, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=cns.CNS_MIXED)
+    err = normwise(U, ref)
+    assert err.max() <= MIXED_TOL, err
+    assert np.allclose(dts, rdt, rtol=1e-6)
+
+
+def test_mixed_128cube_100_steps_vs_fp64(gpu, cns):
+    """Mixed form against the (oracle-validated) FP64 form: 128^3, 100 steps, <= 1e-6."""
+    n = 128
+    U0 = I.initial_state(n, perturb=1e-3, seed=1)
+    out = {}
+    for prec in (cns.CNS_FP64, cns.CNS_MIXED):
+        b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
+        b.upload(U0)
+        b.advance(100)
+        b.sync()
+        out[prec] = b.download()
+        b.close()
+    err = normwise(out[cns.CNS_MIXED], out[cns.CNS_FP64])
+    assert err.max() <= MIXED_TOL, err
