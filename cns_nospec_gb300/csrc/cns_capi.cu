@@ -252,6 +252,7 @@ extern "C" int cns_box_set_stream(cns_box* b, void* stream) {
 // Prime a box whose U interior was just written: primitives/fluxes, Courant, first dt.
 static int prime(cns_box* b) {
     CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
+    CK(launch_refs(b->d_view, 1, b->stream));
     CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->geo.ntiles, b->stream));
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;

@@ -69,6 +69,12 @@ struct BoxScalars {
     int nsteps_done;
     int status;                      // HEALTH_* bits, sticky
     int pad;
+    // Reference values of the mixed form, fixed at upload from one cell of the state (FP64):
+    // the FP32 stencil fields carry p - p_ref, T - T_ref and (E + p) - H_ref, whose rounding
+    // is ~10-30x smaller than that of p, T, E + p themselves.  Every difference operator
+    // annihilates a constant, and the energy flux splits exactly as
+    // d((E+p) u)/dx = H_ref du/dx + d(((E+p) - H_ref) u)/dx.
+    double p_ref, e_ref, E_ref, H_ref;
 };
 
 constexpr int DTLOG_CAP = 1024;

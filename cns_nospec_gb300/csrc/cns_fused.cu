@@ -137,6 +137,12 @@ __global__ void __launch_bounds__(TI* TJ* TK) k_assemble(const BoxView* __restri
             f[4] = d1acc(de, Pr + PHU * fs + c, si, cf.ha[0]);
             f[4] = d1acc(f[4], Pr + PHV * fs + c, sj, cf.ha[1]);
             f[4] = d1acc(f[4], Pr + PHW * fs + c, 1, cf.ha[2]);
+            if (sizeof(R) == 4) {
+                // mixed form: the P set holds ((E + p) - H_ref) u_d, so add -H_ref div(u);
+                // div(u) = (S_x + S_y + S_z) / 2 with the same first-difference operator
+                const R divu = (R)0.5 * (ld(S + SX * fs + c) + ld(S + SY * fs + c) + ld(S + SZ * fs + c));
+                f[4] = fma(-(R)b.sc->H_ref, divu, f[4]);
+            }
             // RK3 stage combine in FP64 (cpu/advance.cpp:78-85, 110-119, 144-153)
             const double dt = b.sc->dt;
             double un[5];
@@ -160,6 +166,23 @@ __global__ void __launch_bounds__(TI* TJ* TK) k_assemble(const BoxView* __restri
         if (health) atomicOr(&b.sc->status, health);
         if (STAGE == 3) courant_fold(b, cour);
     }
+}
+
+// ---- k_refs: the mixed form's reference values from interior cell (0,0,0) of U ----------
+__global__ void k_refs(const BoxView* __restrict__ boxes, int nboxes) {
+    const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bx >= nboxes) return;
+    const BoxView& b = boxes[bx];
+    const long long c = cell_off(b, 0, 0, 0);
+    const double rho = b.U[c], E = b.U[c + 4 * b.fs];
+    const double rinv = 1.0 / rho;
+    const double u = b.U[c + b.fs] * rinv, v = b.U[c + 2 * b.fs] * rinv, w = b.U[c + 3 * b.fs] * rinv;
+    const double eint = E * rinv - 0.5 * (u * u + v * v + w * w);
+    const double p = kGm1 * eint * rho;
+    b.sc->p_ref = p;
+    b.sc->e_ref = eint;
+    b.sc->E_ref = E;
+    b.sc->H_ref = E + p;
 }
 
 // ---- k_stepend: dt for the next step from the Courant max (cpu/advance.cpp:52-58) ----------
@@ -241,6 +264,11 @@ cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* til
     if (ntiles <= 0) return cudaSuccess;
     return precision ? launch_assemble_t<float>(boxes, tiles, ntiles, stage, st)
                      : launch_assemble_t<double>(boxes, tiles, ntiles, stage, st);
+}
+cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st) {
+    if (nboxes <= 0) return cudaSuccess;
+    k_refs<<<(nboxes + 127) / 128, 128, 0, st>>>(boxes, nboxes);
+    return cudaGetLastError();
 }
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st) {
     if (nboxes <= 0) return cudaSuccess;

@@ -98,8 +98,8 @@ __device__ __forceinline__ int health_bits(double rho, double eint) {
 // ctoprim + flux functions of one cell's FP64 conserved state, written to the P set `Pw`
 // with the periodic face images each field's stencils need.  Returns the cell's Courant
 // number (only formed when `want_cour`).  Plain form: everything in FP64 (reciprocal by
-// rcp_nr).  Mixed form: E/rho and the subtraction e = E/rho - |u|^2/2 in FP64, the rest in
-// FP32.
+// rcp_nr).  Mixed form: E/rho, the subtraction e = E/rho - |u|^2/2 and the offsets
+// p - p_ref, T - T_ref, E - E_ref in FP64; the rest in FP32 (see BoxScalars).
 template <class R>
 __device__ __forceinline__ double epilogue(const BoxView& b, R* __restrict__ Pw, long long c, int i, int j, int k,
                                            const double un[5], bool want_cour, int* health);
@@ -156,27 +156,30 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
     const double erho = fma(fma(-rho, y0, E), r64, y0);
     const float ke = fmaf(u, u, fmaf(v, v, w * w));
     const double eint = fma(-0.5, (double)ke, erho);  // the cancelling subtraction, in FP64
-    const float ef = (float)eint;
-    const float p = ((float)kGm1 * ef) * rhof;
-    const float T = ef * (float)(1.0 / kCv);
-    const float H = (float)E + p;
+    // offsets from the box's reference values, formed in FP64 before rounding to FP32
+    const BoxScalars& sc = *b.sc;
+    const double pd = fma(kGm1 * rho, eint, -sc.p_ref);       // p - p_ref
+    const float dp = (float)pd;
+    const float dT = (float)((eint - sc.e_ref) * (1.0 / kCv)); // T - T_ref
+    const float dH = (float)(E - sc.E_ref) + dp;               // (E + p) - H_ref
     *health |= health_bits(rho, eint);
     store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
     store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
     store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
-    store_img(Pw + PT * fs, b, c, i, j, k, T, 7);
+    store_img(Pw + PT * fs, b, c, i, j, k, dT, 7);
     store_img(Pw + PMX * fs, b, c, i, j, k, mx, 1);
     store_img(Pw + PMY * fs, b, c, i, j, k, my, 2);
     store_img(Pw + PMZ * fs, b, c, i, j, k, mz, 4);
-    store_img(Pw + PFUU * fs, b, c, i, j, k, fmaf(mx, u, p), 1);
-    store_img(Pw + PFVV * fs, b, c, i, j, k, fmaf(my, v, p), 2);
-    store_img(Pw + PFWW * fs, b, c, i, j, k, fmaf(mz, w, p), 4);
+    store_img(Pw + PFUU * fs, b, c, i, j, k, fmaf(mx, u, dp), 1);
+    store_img(Pw + PFVV * fs, b, c, i, j, k, fmaf(my, v, dp), 2);
+    store_img(Pw + PFWW * fs, b, c, i, j, k, fmaf(mz, w, dp), 4);
     store_img(Pw + PFUV * fs, b, c, i, j, k, mx * v, 3);
     store_img(Pw + PFUW * fs, b, c, i, j, k, mx * w, 5);
     store_img(Pw + PFVW * fs, b, c, i, j, k, my * w, 6);
-    store_img(Pw + PHU * fs, b, c, i, j, k, H * u, 1);
-    store_img(Pw + PHV * fs, b, c, i, j, k, H * v, 2);
-    store_img(Pw + PHW * fs, b, c, i, j, k, H * w, 4);
+    store_img(Pw + PHU * fs, b, c, i, j, k, dH * u, 1);
+    store_img(Pw + PHV * fs, b, c, i, j, k, dH * v, 2);
+    store_img(Pw + PHW * fs, b, c, i, j, k, dH * w, 4);
+    const float p = (float)(pd + sc.p_ref);
     if (!want_cour) return 0.0;
     const float cs = sqrtf(((float)kGamma * p) * rf);
     const float cx = (cs + fabsf(u)) * b.c32.cour[0];

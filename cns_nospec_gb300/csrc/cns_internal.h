@@ -12,6 +12,7 @@ cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles,
                          cudaStream_t st);
 cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
                             cudaStream_t st);
+cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st);
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st);
 
 // operator-level kernels and layout conversions (cns_ops.cu)
