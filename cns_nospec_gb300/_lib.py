@@ -70,6 +70,15 @@ SIGNATURES = {
     "cns_box_sync": (C.c_int, [_VP, _I]),
     "cns_box_last_dt": (C.c_int, [_VP, _D, _I]),
     "cns_box_launches_per_step": (C.c_int, [_VP]),
+    "cns_box_init_field": (C.c_int, [_VP, _D, C.c_double, C.c_ulonglong]),
+    "cns_box_save": (C.c_int, [_VP, C.c_char_p]),
+    "cns_box_load": (C.c_int, [_VP, C.c_char_p]),
+    "cns_read_general_input": (C.c_int, [C.c_char_p, C.POINTER(GlobalConst)]),
+    "cns_write_general_input": (C.c_int, [C.c_char_p, C.POINTER(GlobalConst)]),
+    "cns_read_3d": (C.c_int, [C.c_char_p, _D, _I, C.c_int]),
+    "cns_write_3d": (C.c_int, [C.c_char_p, _D, _I, C.c_int]),
+    "cns_print_4d": (C.c_int, [C.c_char_p, _D, _I, C.c_int, C.c_int]),
+    "cns_read_4d": (C.c_int, [C.c_char_p, _D, _I, C.c_int, C.c_int]),
     "cns_batch_create": (C.c_int, [C.POINTER(_VP)]),
     "cns_batch_destroy": (C.c_int, [_VP]),
     "cns_batch_set_stream": (C.c_int, [_VP, _VP]),

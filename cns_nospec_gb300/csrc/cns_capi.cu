@@ -40,6 +40,10 @@ static int fail_cuda(cudaError_t e, const char* what, int line) {
     } while (0)
 
 extern "C" const char* cns_last_error(void) { return g_err.c_str(); }
+int cns::set_error(int code, const char* msg) {
+    g_err = msg;
+    return code;
+}
 extern "C" int cns_version(void) { return 100; }
 extern "C" int cns_set_device(int device) {
     CK(cudaSetDevice(device));
@@ -250,14 +254,37 @@ extern "C" int cns_box_set_stream(cns_box* b, void* stream) {
 }
 
 // Prime a box whose U interior was just written: primitives/fluxes, Courant, first dt.
-static int prime(cns_box* b) {
-    CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
-    CK(launch_refs(b->d_view, 1, b->stream));
+// `restore` (a snapshot's scalars) keeps its step count and reference values instead of
+// deriving fresh ones, so a resumed run continues bit for bit.
+static int prime(cns_box* b, const BoxScalars* restore = nullptr) {
+    if (restore) {
+        BoxScalars s;
+        memset(&s, 0, sizeof s);
+        s.nsteps_done = restore->nsteps_done;
+        s.dt_last = restore->dt_last;
+        s.p_ref = restore->p_ref;
+        s.e_ref = restore->e_ref;
+        s.E_ref = restore->E_ref;
+        s.H_ref = restore->H_ref;
+        CK(cudaMemcpyAsync(b->d_sc, &s, sizeof s, cudaMemcpyHostToDevice, b->stream));
+        CK(cudaStreamSynchronize(b->stream));  // s lives on this stack frame
+    } else {
+        CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
+        CK(launch_refs(b->d_view, 1, b->stream));
+    }
     CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->geo.ntiles, b->stream));
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return CNS_OK;
 }
+
+extern "C" int cns_box_init_field(cns_box* b, const double amp[3], double perturb, unsigned long long seed) {
+    if (!b || !amp) return fail(CNS_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(b->dev));
+    CK(op_init_field(b->view, amp[0], amp[1], amp[2], perturb, seed, b->stream));
+    return prime(b);
+}
+
 
 static size_t aos_bytes(const cns_box* b) {
     return sizeof(double) * CNS_NC * (size_t)(b->desc.n[0] + 8) * (b->desc.n[1] + 8) * (b->desc.n[2] + 8);
@@ -842,4 +869,86 @@ extern "C" int cns_new_advance(const cns_global_const_t* h, double* U, double* U
     int rc = cns_advance_host(U, h->dim, h->dx, h->cfl, h->eta, h->alam, 1, CNS_FP64, &dt1);
     if (rc == CNS_OK && dt) *dt = dt1;
     return rc;
+}
+
+// ---- binary snapshot: header + ghost-inclusive AoS state --------------------------------
+struct SnapHeader {
+    char magic[8];  // "CNSSNAP1"
+    int32_t version, precision, n[3], ng;
+    int64_t nsteps_done;
+    double dx[3], cfl, eta, alam;
+    double p_ref, e_ref, E_ref, H_ref, dt_last;
+    int64_t payload_doubles;
+};
+
+extern "C" int cns_box_save(cns_box* b, const char* path) {
+    if (!b || !path) return fail(CNS_ERR_INVALID, "null argument");
+    if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state");
+    CK(cudaSetDevice(b->dev));
+    std::vector<double> U(aos_bytes(b) / sizeof(double));
+    BoxScalars hs;
+    int rc = cns_box_download(b, U.data());
+    if (rc) return rc;
+    if ((rc = read_scalars(b, &hs))) return rc;
+    SnapHeader h;
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, "CNSSNAP1", 8);
+    h.version = 1;
+    h.precision = b->desc.precision;
+    for (int a = 0; a < 3; a++) {
+        h.n[a] = b->desc.n[a];
+        h.dx[a] = b->desc.dx[a];
+    }
+    h.ng = CNS_NG;
+    h.nsteps_done = hs.nsteps_done;
+    h.cfl = b->desc.cfl;
+    h.eta = b->desc.eta;
+    h.alam = b->desc.alam;
+    h.p_ref = hs.p_ref;
+    h.e_ref = hs.e_ref;
+    h.E_ref = hs.E_ref;
+    h.H_ref = hs.H_ref;
+    h.dt_last = hs.dt_last;
+    h.payload_doubles = (int64_t)U.size();
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(CNS_ERR_INVALID, "cannot create %s", path);
+    bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(U.data(), sizeof(double), U.size(), f) == U.size();
+    ok = (fclose(f) == 0) && ok;
+    return ok ? CNS_OK : fail(CNS_ERR_INVALID, "short write to %s", path);
+}
+
+extern "C" int cns_box_load(cns_box* b, const char* path) {
+    if (!b || !path) return fail(CNS_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(b->dev));
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(CNS_ERR_INVALID, "cannot open %s", path);
+    SnapHeader h;
+    std::vector<double> U(aos_bytes(b) / sizeof(double));
+    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "CNSSNAP1", 8) == 0 && h.version == 1;
+    if (ok) {
+        ok = h.precision == b->desc.precision && h.ng == CNS_NG && h.payload_doubles == (int64_t)U.size();
+        for (int a = 0; a < 3; a++) ok = ok && h.n[a] == b->desc.n[a] && h.dx[a] == b->desc.dx[a];
+        ok = ok && h.cfl == b->desc.cfl && h.eta == b->desc.eta && h.alam == b->desc.alam;
+        if (!ok) {
+            fclose(f);
+            return fail(CNS_ERR_INVALID, "snapshot %s does not match this box (dims, dx, params or precision)", path);
+        }
+        ok = fread(U.data(), sizeof(double), U.size(), f) == U.size();
+    }
+    fclose(f);
+    if (!ok) return fail(CNS_ERR_INVALID, "%s is not a complete snapshot", path);
+    CK(cudaMemcpyAsync(b->d_aos, U.data(), aos_bytes(b), cudaMemcpyHostToDevice, b->stream));
+    CK(op_aos_to_box(b->d_aos, b->view, b->stream));
+    BoxScalars s;
+    memset(&s, 0, sizeof s);
+    s.nsteps_done = (int)h.nsteps_done;
+    s.dt_last = h.dt_last;
+    s.p_ref = h.p_ref;
+    s.e_ref = h.e_ref;
+    s.E_ref = h.E_ref;
+    s.H_ref = h.H_ref;
+    int rc = prime(b, &s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    return CNS_OK;
 }

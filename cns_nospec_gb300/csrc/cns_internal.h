@@ -5,6 +5,9 @@
 
 namespace cns {
 
+// record the calling thread's last error (read back by cns_last_error); returns `code`
+int set_error(int code, const char* msg);
+
 // fused RK3 stage kernels (cns_fused.cu); precision 0 = FP64 stencils, 1 = FP32 stencils
 void tile_shape(int* ti, int* tj, int* tk);
 cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st);
@@ -28,5 +31,7 @@ cudaError_t op_fill_ghosts_aos(double* aos, const int n[3], int nc, cudaStream_t
 cudaError_t op_aos_to_box(const double* aos, const BoxView& b, cudaStream_t st);
 cudaError_t op_box_to_aos(const BoxView& b, double* aos, int ghosts, cudaStream_t st);
 cudaError_t probe_fp64(double* tflops);
+cudaError_t op_init_field(const BoxView& b, double ax, double ay, double az, double perturb, unsigned long long seed,
+                          cudaStream_t st);
 
 }  // namespace cns

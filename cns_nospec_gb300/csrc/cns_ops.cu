@@ -338,3 +338,54 @@ cudaError_t probe_fp64(double* tflops) {
     return e;
 }
 }  // namespace cns
+
+// ---- the CNS_NoSpec initial field generated on the device (serving requests) -------------
+// Same field and perturbation stream as cns_nospec_gb300/initdata.py: cell-centred
+// X = 2 pi (i + 1/2) / n0 etc., velocity amplitudes scaled by (ax, ay, az), rho, u, v, w times
+// (1 + perturb * (2 U - 1)) with U from SplitMix64 at counter ((i*n1 + j)*n2 + k)*4 + field.
+namespace cns {
+__device__ __forceinline__ double splitmix_uniform(unsigned long long counter, unsigned long long seed) {
+    unsigned long long z = counter + seed * 0x9E3779B97F4A7C15ull + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__global__ void k_init_field(BoxView b, double ax, double ay, double az, double perturb, unsigned long long seed) {
+    const long long nint = (long long)b.n[0] * b.n[1] * b.n[2];
+    const double twopi = 6.283185307179586476925286766559;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nint; p += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(p % b.n[2]);
+        const int j = (int)((p / b.n[2]) % b.n[1]);
+        const int i = (int)(p / ((long long)b.n[2] * b.n[1]));
+        const double X = twopi * (i + 0.5) / b.n[0], Y = twopi * (j + 0.5) / b.n[1], Z = twopi * (k + 0.5) / b.n[2];
+        double u = (1.1e4 * ax) * (sin(X) * sin(2 * Y) * sin(3 * Z));
+        double v = (1.0e4 * ay) * (sin(2 * X) * sin(4 * Y) * sin(Z));
+        double w = (1.2e4 * az) * (sin(3 * X) * cos(2 * Y) * sin(2 * Z));
+        double rho = 1.0e-3 + 1.0e-5 * (sin(X) * cos(2 * Y) * cos(3 * Z));
+        const double e = 2.5e9 + 1.0e-3 * (sin(X) * cos(2 * Y) * sin(2 * Z));
+        if (perturb != 0.0) {
+            const unsigned long long cnt = (unsigned long long)p * 4ull;
+            rho *= 1.0 + perturb * (2.0 * splitmix_uniform(cnt, seed) - 1.0);
+            u *= 1.0 + perturb * (2.0 * splitmix_uniform(cnt + 1, seed) - 1.0);
+            v *= 1.0 + perturb * (2.0 * splitmix_uniform(cnt + 2, seed) - 1.0);
+            w *= 1.0 + perturb * (2.0 * splitmix_uniform(cnt + 3, seed) - 1.0);
+        }
+        const long long c = cell_off(b, i, j, k);
+        b.U[c] = rho;
+        b.U[c + b.fs] = rho * u;
+        b.U[c + 2 * b.fs] = rho * v;
+        b.U[c + 3 * b.fs] = rho * w;
+        b.U[c + 4 * b.fs] = rho * (e + (u * u + v * v + w * w) / 2.0);
+    }
+}
+
+cudaError_t op_init_field(const BoxView& b, double ax, double ay, double az, double perturb, unsigned long long seed,
+                          cudaStream_t st) {
+    const long long nint = (long long)b.n[0] * b.n[1] * b.n[2];
+    long long blocks = (nint + 255) / 256;
+    k_init_field<<<(int)(blocks > 4096 ? 4096 : blocks), 256, 0, st>>>(b, ax, ay, az, perturb, seed);
+    return cudaGetLastError();
+}
+}  // namespace cns

@@ -146,6 +146,17 @@ class Box:
             raise ValueError(f"U has shape {U.shape}, expected {self.shape()}")
         L.check(self.lib.cns_box_upload(self.h, L.dptr(U)))
 
+    def init_field(self, amp=(1.0, 1.0, 1.0), perturb=0.0, seed=1):
+        """Generate the CNS_NoSpec initial field on the device (no host array)."""
+        a = (C.c_double * 3)(*[float(x) for x in amp])
+        L.check(self.lib.cns_box_init_field(self.h, a, float(perturb), C.c_ulonglong(int(seed))))
+
+    def save(self, path):
+        L.check(self.lib.cns_box_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        L.check(self.lib.cns_box_load(self.h, str(path).encode()))
+
     def download(self, out=None):
         out = np.empty(self.shape(), dtype=np.float64) if out is None else _f64(out, "out")
         L.check(self.lib.cns_box_download(self.h, L.dptr(out)))

@@ -139,6 +139,30 @@ int cns_box_last_dt(cns_box *box, double *dt, int *nsteps_done);
 /* Kernel launches one cns_box_advance step issues (for launch accounting). */
 int cns_box_launches_per_step(const cns_box *box);
 
+/* Write the CNS_NoSpec initial field straight into the box (no host array): velocity
+ * amplitudes scaled by amp[3], rho/u/v/w times (1 + perturb * U(-1, 1)) from the seeded
+ * SplitMix64 stream of cns_nospec_gb300/initdata.py; then primes the box like an upload. */
+int cns_box_init_field(cns_box *box, const double amp[3], double perturb, unsigned long long seed);
+/* Checkpoint / resume: a binary snapshot (header + ghost-inclusive AoS state + the box's
+ * step count and mixed-form reference values).  Loading into a box of the same description
+ * resumes the run bit for bit.  Both block. */
+int cns_box_save(cns_box *box, const char *path);
+int cns_box_load(cns_box *box, const char *path);
+
+/* ---- the reference's text formats (host only) ------------------------------------------ */
+/* general_input: "ng nc ncells lo[3] hi[3] dx[3] cfl eta alam nsteps dt", derived fields as in
+ * read_configurations (cpu/helper_functions.cpp:38-83). */
+int cns_read_general_input(const char *path, cns_global_const_t *h);
+int cns_write_general_input(const char *path, const cns_global_const_t *h);
+/* ncomp components as read_3D reads them (cpu/helper_functions.cpp:166-175), i fastest, into
+ * / from an [d0][d1][d2][ncomp] block (the multistep_input format, cpu/main.cpp:22-25). */
+int cns_read_3d(const char *path, double *a, const int dims[3], int ncomp);
+int cns_write_3d(const char *path, const double *a, const int dims[3], int ncomp);
+/* print_4D dumps (cpu/helper_functions.cpp:85-98), "%.17e\t" per value; with_header adds the
+ * two header lines cpu/main.cpp:36-40 writes before it (ncomp; the three dims). */
+int cns_print_4d(const char *path, const double *a, const int dims[3], int ncomp, int with_header);
+int cns_read_4d(const char *path, double *a, const int dims[3], int ncomp, int with_header);
+
 /* ---- batches: many boxes advanced together, one launch per kernel and stage ------------ */
 typedef struct cns_batch cns_batch;
 int cns_batch_create(cns_batch **out);

@@ -173,3 +173,38 @@ int ref_diffterm(const int lo_in[3], const int hi_in[3], int ng, const double dx
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// cpu/helper_functions.cpp:85-98 print_4D into a file (dims as given, dl components).
+int ref_print_4D(const char *path, double *A, const int dims[3], int dl) {
+    FILE *f = fopen(path, "w");
+    if (!f) return 1;
+    int d[3] = {dims[0], dims[1], dims[2]};
+    Tree4 t(A, d[0], d[1], d[2], dl);
+    print_4D(f, t.p, d, dl);
+    fclose(f);
+    return 0;
+}
+
+// cpu/helper_functions.cpp:166-175 read_3D of dl components from a file.
+int ref_read_3D(const char *path, double *A, const int dims[3], int dl) {
+    FILE *f = fopen(path, "r");
+    if (!f) return 1;
+    int d[3] = {dims[0], dims[1], dims[2]};
+    Tree4 t(A, d[0], d[1], d[2], dl);
+    for (int l = 0; l < dl; l++) read_3D(f, t.p, d, l);
+    fclose(f);
+    return 0;
+}
+
+// cpu/helper_functions.cpp:38-83 read_configurations, which opens ../testcases/general_input
+// relative to the working directory; the caller chdirs accordingly.  Copies h_const out.
+int ref_read_configurations(void *out, int out_size) {
+    if (out_size != (int)sizeof(global_const_t)) return 1;
+    read_configurations(h_const);
+    memcpy(out, &h_const, sizeof(global_const_t));
+    return 0;
+}
+
+}  // extern "C"
