@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--n", type=int, default=128, help="cells per axis of the periodic box")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    p.add_argument("--case", choices=["fp64", "mixed"], default=None,
+                   help="profiling case: only upload + warmup + steps of one form (for ncu), then exit")
     return p.parse_args()
 
 
@@ -329,8 +331,28 @@ def Box_bytes(C, n):
     return C.Box.bytes_for(n, C.CNS_FP64)
 
 
+def run_case(args):
+    """Just the kernels of one form on the n^3 box: what an ncu capture should see."""
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    from cns_nospec_gb300 import initdata as I
+    lib = C.load()
+    L.check(lib.cns_set_device(0))
+    prec = C.CNS_FP64 if args.case == "fp64" else C.CNS_MIXED
+    box = C.Box(args.n, I.box_dx(args.n), I.CFL, I.ETA, I.ALAM, precision=prec)
+    box.init_field(perturb=1e-3, seed=1)
+    box.advance_timed(args.warmup)
+    ms, launches, total = box.advance_timed(args.steps)
+    box.sync()
+    print(json.dumps({"case": args.case, "n": args.n, "steps": args.steps, "total_ms": total,
+                      "kernel_ms": dict(zip(L.KERNEL_NAMES, ms)), "launches": dict(zip(L.KERNEL_NAMES, launches))}))
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args)
+        return
     dist = Dist()
     try:
         if args.impl == "reference":

@@ -59,6 +59,23 @@ extern "C" int cns_measure_fp64_peak(double* tflops) {
     return CNS_OK;
 }
 
+// Keep freed box memory in the device's default pool instead of returning it to the driver
+// at each synchronisation, so that admitting a box after another finished costs no driver
+// allocation.
+static cudaError_t keep_pool_warm(int dev) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), dev) != done.end()) return cudaSuccess;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    if (e != cudaSuccess) return e;
+    unsigned long long thr = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (e == cudaSuccess) done.push_back(dev);
+    return e;
+}
+
 // ---- geometry and coefficients ----------------------------------------------------------
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -181,8 +198,10 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     b->desc = *desc;
     b->geo = geometry(desc);
     cudaError_t e = cudaGetDevice(&b->dev);
+    if (e == cudaSuccess) e = keep_pool_warm(b->dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->arena, b->geo.total);
+    // stream-ordered allocation: freeing a finished box later needs no device-wide sync
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&b->arena, b->geo.total, b->own_stream);
     if (e != cudaSuccess) {
         if (b->own_stream) cudaStreamDestroy(b->own_stream);
         delete b;
@@ -224,7 +243,8 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
         e = cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {
-        cudaFree(b->arena);
+        cudaFreeAsync(b->arena, b->own_stream);
+        cudaStreamSynchronize(b->own_stream);
         cudaStreamDestroy(b->own_stream);
         delete b;
         return fail_cuda(e, "cns_box_create init", __LINE__);
@@ -235,14 +255,24 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
 
 extern "C" int cns_batch_remove(cns_batch* batch, cns_box* box);
 
+static cudaStream_t batch_stream(cns_batch* bt);
+
 extern "C" int cns_box_destroy(cns_box* b) {
     if (!b) return CNS_OK;
     cudaSetDevice(b->dev);
-    if (b->batch) cns_batch_remove(b->batch, b);
-    cudaStreamSynchronize(b->stream);
+    if (b->batch) {
+        // work already queued by the batch may still touch this box: order the free after it
+        cudaEvent_t ev;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(ev, batch_stream(b->batch));
+            cudaStreamWaitEvent(b->stream, ev, 0);
+            cudaEventDestroy(ev);
+        }
+        cns_batch_remove(b->batch, b);
+    }
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
-    cudaFree(b->arena);
-    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    cudaFreeAsync(b->arena, b->stream);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);  // released once its queued work is done
     delete b;
     return CNS_OK;
 }
@@ -492,6 +522,8 @@ struct cns_batch {
     bool dirty = true;
     cudaGraphExec_t gexec = nullptr;
 };
+
+static cudaStream_t batch_stream(cns_batch* bt) { return bt->stream; }
 
 extern "C" int cns_batch_create(cns_batch** out) {
     if (!out) return fail(CNS_ERR_INVALID, "null output handle");

@@ -153,3 +153,36 @@ def advance(U: np.ndarray, nsteps: int, dx, cfl: float, eta: float, alam: float,
         _lib("ref").ref_new_advance(_dp(U), int(dims[0]), _dv(dx), float(cfl), float(eta), float(alam),
                                     int(nsteps), _dp(dts))
     return U, dts[:nsteps]
+
+
+# ---- the reference's own file I/O (oracle/_ref only) ---------------------------------------
+def ref_print_4d(path, A: np.ndarray) -> None:
+    lib = _lib("ref")
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    lib.ref_print_4D.argtypes = [C.c_char_p, _D, _I, C.c_int]
+    if lib.ref_print_4D(str(path).encode(), _dp(A), _ip(A.shape[:3]), int(A.shape[3])) != 0:
+        raise OSError(path)
+
+
+def ref_read_3d(path, dims, ncomp: int) -> np.ndarray:
+    lib = _lib("ref")
+    A = np.zeros(tuple(dims) + (ncomp,), dtype=np.float64)
+    lib.ref_read_3D.argtypes = [C.c_char_p, _D, _I, C.c_int]
+    if lib.ref_read_3D(str(path).encode(), _dp(A), _ip(dims), int(ncomp)) != 0:
+        raise OSError(path)
+    return A
+
+
+def ref_read_configurations(workdir, out_struct) -> None:
+    """Run the reference's read_configurations, which opens ../testcases/general_input
+    relative to the working directory, from `workdir`; fills the ctypes struct `out_struct`."""
+    lib = _lib("ref")
+    lib.ref_read_configurations.argtypes = [C.c_void_p, C.c_int]
+    cwd = os.getcwd()
+    os.chdir(workdir)
+    try:
+        rc = lib.ref_read_configurations(C.addressof(out_struct), C.sizeof(out_struct))
+    finally:
+        os.chdir(cwd)
+    if rc != 0:
+        raise RuntimeError("struct size mismatch")

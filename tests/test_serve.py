@@ -1,0 +1,110 @@
+"""The continuous-batching server: scheduling logic on CPU against a host fake of the device
+backend, and (GPU) the real thing, including alone == in-the-mix bit for bit."""
+import numpy as np
+import pytest
+
+from cns_nospec_gb300 import serve as S
+
+
+class FakeBox:
+    """Host stand-in with the Box interface the server uses; 'bytes' = cells."""
+    live = []
+
+    def __init__(self, n, dx, cfl, eta, alam, precision=0):
+        self.n, self.prec, self.steps = n, precision, 0
+        FakeBox.live.append(self)
+
+    @staticmethod
+    def bytes_for(n, precision=0):
+        return n[0] * n[1] * n[2]
+
+    def init_field(self, amp, perturb, seed):
+        self.seed = seed
+
+    def sync(self):
+        pass
+
+    def download(self):
+        return np.full(1, float(self.steps))
+
+    def close(self):
+        if self in FakeBox.live:
+            FakeBox.live.remove(self)
+
+
+class FakeBatch:
+    def __init__(self):
+        self.members = []
+        self.max_members = 0
+
+    def add(self, b):
+        self.members.append(b)
+        self.max_members = max(self.max_members, len(self.members))
+
+    def remove(self, b):
+        self.members.remove(b)
+
+    def advance(self, k=1):
+        for b in self.members:
+            b.steps += k
+
+    def sync(self):
+        pass
+
+    def close(self):
+        self.members = []
+
+
+def test_request_stream_is_seeded_and_in_range():
+    a = S.request_stream(rate=5.0, count=200, seed=4)
+    b = S.request_stream(rate=5.0, count=200, seed=4)
+    assert [(r.n, r.steps, r.precision, r.arrival) for r in a] == [(r.n, r.steps, r.precision, r.arrival) for r in b]
+    assert all(24 <= r.n[0] <= 192 and 10 <= r.steps <= 200 for r in a)
+    assert all(0.8 <= x <= 1.2 for r in a for x in r.amp)
+    arr = np.array([r.arrival for r in a])
+    assert np.all(np.diff(arr) > 0) and 0.1 < np.diff(arr).mean() < 0.3
+    mixed = sum(r.precision for r in a) / len(a)
+    assert 0.35 < mixed < 0.65
+
+
+def test_server_admits_in_order_within_budget_and_finishes_everything():
+    reqs = [S.Request(i, 0.0, (10, 10, 10), steps, 0) for i, steps in enumerate([5, 3, 8, 2, 6, 4])]
+    srv = S.Server(budget_bytes=2500, keep_results=True, box_cls=FakeBox, batch_cls=FakeBatch)
+    rep = srv.run(reqs, realtime=False)
+    assert rep["requests"] == 6
+    assert rep["peak_bytes"] <= 2500
+    admits = [e["admit"] for e in srv.log]
+    assert admits == sorted(admits)                   # FIFO admission
+    assert max(e["active"] for e in srv.log) == 2     # two 1000-cell boxes fit, a third does not
+    for d in rep["done"]:
+        assert d.result[0] == d.req.steps             # each box got exactly its own steps
+    assert not FakeBox.live                           # every box released
+
+
+def test_server_slot_limit_and_realtime_arrivals():
+    reqs = [S.Request(i, 0.01 * i, (4, 4, 4), 3, i % 2) for i in range(5)]
+    srv = S.Server(budget_bytes=1e9, max_active=2, box_cls=FakeBox, batch_cls=FakeBatch)
+    rep = srv.run(reqs, realtime=True)
+    assert rep["requests"] == 5
+    assert max(e["active"] for e in srv.log) <= 2
+    assert rep["latency_p99_s"] >= rep["latency_p50_s"] >= 0
+
+
+def test_oversized_request_is_refused():
+    reqs = [S.Request(0, 0.0, (100, 100, 100), 3, 0)]
+    with pytest.raises(ValueError):
+        S.Server(budget_bytes=1000, box_cls=FakeBox, batch_cls=FakeBatch).run(reqs, realtime=False)
+    assert not FakeBox.live
+
+
+@pytest.mark.gpu
+def test_served_results_equal_alone_bitwise(gpu, cns):
+    reqs = S.request_stream(rate=50.0, count=6, seed=9, nmin=16, nmax=40, smin=4, smax=12)
+    budget = 2.2 * max(cns.Box.bytes_for(r.n, r.precision) for r in reqs)
+    srv = S.Server(budget_bytes=budget, keep_results=True)
+    rep = srv.run(reqs, realtime=False)
+    assert rep["requests"] == 6
+    assert max(e["active"] for e in srv.log) >= 2      # the work overlapped on the device
+    assert rep["peak_bytes"] <= budget
+    for d in rep["done"]:
+        assert np.array_equal(d.result, S.run_alone(d.req)), d.req
