@@ -54,6 +54,7 @@ SIGNATURES = {
     "cns_ctoprim": (C.c_int, [_I, _I, _D, _D, _D, C.c_int, _D]),
     "cns_hypterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, _D]),
     "cns_diffterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, C.c_double, C.c_double]),
+    "cns_diffterm_noalloc": (C.c_int, [_I, _I, C.c_int, _D, _VP, _VP, C.c_double, C.c_double, _VP]),
     "cns_fill_boundary": (C.c_int, [_D, _I, _I]),
     "cns_new_advance": (C.c_int, [C.POINTER(GlobalConst), _D, _D, _D, _D, _D, _D]),
     "cns_advance_host": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _D]),

@@ -84,6 +84,22 @@ int cns_hypterm(const int lo[3], const int hi[3], int ng, const double dx[3], co
 int cns_diffterm(const int lo[3], const int hi[3], int ng, const double dx[3], const double *q,
                  double *difflux, double eta, double alam);
 
+/* No counterpart in the reference (its diffterm mallocs nine temporaries per call,
+ * cpu/diffterm.cpp:59-61).  diffterm for callers that cannot allocate device memory while
+ * they run (memory owned by another allocator or a fixed budget, or loops that cannot take
+ * cudaMalloc's synchronisation): q_dev ([g0][g1][g2][6]) and difflux_dev ([n0][n1][n2][5]) are
+ * caller-owned DEVICE buffers in the reference layout; the temporaries live in one fixed
+ * device array of CNS_NOALLOC_MAX_POINTS * 20 doubles (10.24 MB), present on every GPU that
+ * loads the library until the process exits.  No cudaMalloc/cudaFree or other allocating call
+ * is made.  Boxes above CNS_NOALLOC_MAX_POINTS ghost-inclusive points return
+ * CNS_ERR_CAPACITY.  Asynchronous on `stream` (NULL = default stream).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress): make it before any
+ * stream capture.  All calls share the array, which keeps the last call's contents (every
+ * element a call reads it first writes); calls that overlap on the GPU race. */
+#define CNS_NOALLOC_MAX_POINTS 64000
+int cns_diffterm_noalloc(const int lo[3], const int hi[3], int ng, const double dx[3], const double *q_dev,
+                         double *difflux_dev, double eta, double alam, void *stream);
+
 /* cpu/helper_functions.cpp:226-262 (helper_functions.h:172-176): periodic ghost fill of a
  * ghost-inclusive [dim+8]^3 x 5 block, in place. */
 int cns_fill_boundary(double *U, const int dim[3], const int dim_ng[3]);
