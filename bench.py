@@ -50,6 +50,16 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     p.add_argument("--case", choices=["fp64", "mixed"], default=None,
                    help="profiling case: only upload + warmup + steps of one form (for ncu), then exit")
+    p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve"], default="box",
+                   help="box: the headline 128^3 line (default); batch: 256 uneven boxes; "
+                        "mixed256: FP64 vs mixed at --n (use 256); serve: the request stream")
+    p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    p.add_argument("--boxes", type=int, default=256)
+    p.add_argument("--rate", type=float, default=3.0, help="serve: requests per second")
+    p.add_argument("--requests", type=int, default=48)
+    p.add_argument("--budget-gb", type=float, default=120.0)
+    p.add_argument("--big", type=int, default=512, help="serve: the single box run alone beside the stream")
+    p.add_argument("--big-steps", type=int, default=3)
     return p.parse_args()
 
 
@@ -231,6 +241,7 @@ def run_ours(args, dist):
     # ---- device-resident FP64 plain form: the headline value --------------------------------
     box = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_FP64)
     box.upload(U0)
+    tile64, _ = box.autotune(trial_steps=2)  # state restored afterwards
     box.advance_timed(args.warmup)
     lib.cns_device_synchronize()
     dist.barrier()
@@ -249,13 +260,23 @@ def run_ours(args, dist):
     # ---- mixed form on the same box ----------------------------------------------------------
     mbox = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_MIXED)
     mbox.upload(U0)
+    tile32, _ = mbox.autotune(trial_steps=2)
     mbox.advance_timed(args.warmup)
     mms, _, mtotal = mbox.advance_timed(args.steps)
     mbox.sync()
-    Umix = mbox.download()
     mbox.close()
-    mixed_err = I.normwise_error(Umix, U64)[0]
     mixed_value = cells * args.steps / (mtotal * 1e-3)
+    # error of the mixed form against FP64 after exactly 100 RK3 steps from the same state
+    ends = {}
+    for prec in (C.CNS_FP64, C.CNS_MIXED):
+        eb = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=prec)
+        eb.upload(U0)
+        eb.advance(100)
+        eb.sync()
+        ends[prec] = eb.download()
+        eb.close()
+    mixed_err = I.normwise_error(ends[C.CNS_MIXED], ends[C.CNS_FP64])[0]
+    del U64
 
     # ---- end to end through the reference-facing C ABI: host buffers, copies timed ----------
     h = C.read_configurations(n, dx, I.CFL, I.ETA, I.ALAM)
@@ -302,7 +323,8 @@ def run_ours(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"periodic box {n}^3 + 4 ghosts, FP64 plain RK3 (config 1 field, seed 1)",
                    "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
-                   "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)"},
+                   "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
+                   "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)}},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "api": "cns_new_advance (host U, copy in + 1 step + copy out)",
                 "pinned_host": pinned, "steps": k_e2e},
@@ -317,7 +339,7 @@ def run_ours(args, dist):
                       "frac_of_fp64_peak": FLOPS_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e12 / fp64_peak},
         "kernels_ms_per_step": {names[i]: kms[i] / args.steps for i in range(L.KERN_COUNT)},
         "mixed": {"value": mixed_value, "unit": "cell-updates/s", "speedup_vs_fp64": mixed_value / (value / dist.world),
-                  "max_normwise_err_vs_fp64": float(mixed_err.max()),
+                  "max_normwise_err_vs_fp64_after_100_steps": float(mixed_err.max()),
                   "err_per_var": [float(x) for x in mixed_err], "steps": args.steps,
                   "kernels_ms_per_step": {names[i]: mms[i] / args.steps for i in range(L.KERN_COUNT)}},
         "gpu_launches": int(sum(klaunch)),
@@ -348,10 +370,138 @@ def run_case(args):
                       "kernel_ms": dict(zip(L.KERNEL_NAMES, ms)), "launches": dict(zip(L.KERNEL_NAMES, launches))}))
 
 
+def batch_specs(count=256, seed=2, nmin=16, nmax=96):
+    """Uneven periodic boxes: per-axis sizes log-uniform over [nmin, nmax], velocity
+    amplitudes, eta and alam x U(0.8, 1.2), seeded (numpy PCG64)."""
+    import math
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for b in range(count):
+        n = tuple(int(round(math.exp(x))) for x in rng.uniform(math.log(nmin), math.log(nmax), 3))
+        amp = tuple(float(x) for x in rng.uniform(0.8, 1.2, 3))
+        f_eta, f_alam = (float(x) for x in rng.uniform(0.8, 1.2, 2))
+        out.append((n, amp, f_eta, f_alam, 100 + b))
+    return out
+
+
+def run_batch(args):
+    """256 uneven boxes (16..96 cells per axis), 50 RK3 steps, one persistent launch per kernel
+    and stage for all boxes, the step captured in a CUDA graph, tile shapes autotuned."""
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    from cns_nospec_gb300 import initdata as I
+    lib = C.load()
+    L.check(lib.cns_set_device(0))
+    prec = C.CNS_MIXED if args.precision == "mixed" else C.CNS_FP64
+    specs = batch_specs(args.boxes)
+    boxes, cells = [], 0
+    batch = C.Batch()
+    for n, amp, fe, fa, seed in specs:
+        b = C.Box(n, I.box_dx(n), I.CFL, I.ETA * fe, I.ALAM * fa, precision=prec)
+        b.init_field(amp, 1e-3, seed)
+        batch.add(b)
+        boxes.append(b)
+        cells += n[0] * n[1] * n[2]
+    t0 = time.perf_counter()
+    policy, tuned_ms = batch.autotune(trial_steps=2)
+    tune_s = time.perf_counter() - t0
+    batch.advance(args.warmup)
+    batch.sync()
+    t0 = time.perf_counter()
+    batch.advance(args.steps)
+    batch.sync()
+    el = time.perf_counter() - t0
+    for b in boxes:
+        b.sync()
+    value = cells * args.steps / el
+    # the first 32 boxes one at a time (each its own graph), for the batching efficiency
+    solo_cells, solo_t = 0, 0.0
+    for b, (n, *_r) in zip(boxes[:32], specs[:32]):
+        batch.remove(b)
+        b.advance(1)
+        b.sync()
+        ts = time.perf_counter()
+        b.advance(5)
+        b.sync()
+        solo_t += time.perf_counter() - ts
+        solo_cells += n[0] * n[1] * n[2] * 5
+    res = {"workload": f"batch of {len(boxes)} uneven periodic boxes (16..96 per axis, seed 2), {args.precision}",
+           "cells_per_step": cells, "steps": args.steps, "value": value, "unit": "cell-updates/s",
+           "ms_per_step": 1e3 * el / args.steps, "autotune_policy": policy,
+           "autotune_ms_per_step_trial": tuned_ms, "autotune_s": tune_s, "launches_per_step": 7,
+           "first32_one_at_a_time_cell_updates_per_s": solo_cells / solo_t,
+           "device_bytes": sum(C.Box.bytes_for(s[0], prec) for s in specs)}
+    batch.close()
+    for b in boxes:
+        b.close()
+    return res
+
+
+def run_mixed256(args):
+    """256^3 box, config-1 field: FP64 and mixed forms, 100 RK3 steps each; normwise error
+    of the mixed form against FP64 per conserved variable, and cell-updates/s of both."""
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    from cns_nospec_gb300 import initdata as I
+    lib = C.load()
+    L.check(lib.cns_set_device(0))
+    n = args.n
+    out, rate = {}, {}
+    for prec in (C.CNS_FP64, C.CNS_MIXED):
+        b = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
+        b.init_field((1.0, 1.0, 1.0), 1e-3, 1)
+        ms, launches, total = b.advance_timed(args.steps)
+        b.sync()
+        rate[prec] = n ** 3 * args.steps / (total * 1e-3)
+        out[prec] = b.download()
+        b.close()
+    mx, rms = I.normwise_error(out[C.CNS_MIXED], out[C.CNS_FP64])
+    return {"workload": f"periodic box {n}^3, config-1 field, {args.steps} RK3 steps", "fp64_cell_updates_per_s":
+            rate[C.CNS_FP64], "mixed_cell_updates_per_s": rate[C.CNS_MIXED],
+            "speedup": rate[C.CNS_MIXED] / rate[C.CNS_FP64], "max_normwise_err": [float(x) for x in mx],
+            "rms_normwise_err": [float(x) for x in rms], "vars": ["rho", "rho u", "rho v", "rho w", "rho E"]}
+
+
+def run_serve(args):
+    """Poisson stream of independent solves (n 24..192, 10..200 steps, coefficients x U(0.8,1.2),
+    50/50 FP64/mixed), HBM budget, continuous batching; p50/p99 latency and throughput, beside
+    a single 512^3 FP64 box advanced alone."""
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    from cns_nospec_gb300 import initdata as I
+    from cns_nospec_gb300 import serve as S
+    lib = C.load()
+    L.check(lib.cns_set_device(0))
+    reqs = S.request_stream(rate=args.rate, count=args.requests, seed=4)
+    srv = S.Server(budget_bytes=args.budget_gb * 1e9)
+    rep = srv.run(reqs, realtime=True)
+    sat = S.Server(budget_bytes=args.budget_gb * 1e9).run(
+        S.request_stream(rate=args.rate, count=args.requests, seed=5), realtime=False)
+    big = {}
+    if args.big > 0:
+        n = args.big
+        b = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+        b.init_field((1.0, 1.0, 1.0), 1e-3, 1)
+        ms, _, total = b.advance_timed(args.big_steps)
+        b.sync()
+        big = {"n": n, "steps": args.big_steps, "cell_updates_per_s": n ** 3 * args.big_steps / (total * 1e-3),
+               "device_bytes": C.Box.bytes_for(n)}
+        b.close()
+    strip = lambda r: {k: v for k, v in r.items() if k != "done"}
+    return {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, n 24..192, steps 10..200, "
+                        f"50/50 FP64/mixed, budget {args.budget_gb} GB",
+            "realtime": strip(rep), "saturated": strip(sat), "single_box_alone": big,
+            "max_active": max((e["active"] for e in srv.log), default=0)}
+
+
 def main():
     args = parse()
     if args.case:
         run_case(args)
+        return
+    if args.workload != "box":
+        fn = {"batch": run_batch, "mixed256": run_mixed256, "serve": run_serve}[args.workload]
+        print(json.dumps(fn(args)))
         return
     dist = Dist()
     try:

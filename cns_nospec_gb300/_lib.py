@@ -88,6 +88,10 @@ SIGNATURES = {
     "cns_batch_size": (C.c_int, [_VP]),
     "cns_batch_advance": (C.c_int, [_VP, C.c_int]),
     "cns_batch_sync": (C.c_int, [_VP]),
+    "cns_box_get_tile": (C.c_int, [_VP, _I]),
+    "cns_box_set_tile": (C.c_int, [_VP, _I]),
+    "cns_box_autotune": (C.c_int, [_VP, C.c_int, _I, _D]),
+    "cns_batch_autotune": (C.c_int, [_VP, C.c_int, _I, _D]),
 }
 
 _lib = None

@@ -99,17 +99,48 @@ static int validate_desc(const cns_box_desc* d) {
     return CNS_OK;
 }
 
+// ---- tile shapes ----------------------------------------------------------------------------
+// Candidate tile shapes (log2 of the i, j, k extents; 256 cells each).  k is the unit-stride
+// axis, so every candidate keeps at least 8 consecutive k cells in a warp.
+static const int kShapes[][3] = {{1, 2, 5}, {0, 3, 5}, {2, 1, 5}, {0, 2, 6}, {1, 1, 6},
+                                 {1, 3, 4}, {2, 2, 4}, {0, 4, 4}, {3, 1, 4}, {2, 3, 3}, {3, 2, 3}, {1, 4, 3}};
+static const int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+
+static long long tile_count(const int n[3], const int tlog[3]) {
+    long long c = 1;
+    for (int a = 0; a < 3; a++) c *= (n[a] + (1 << tlog[a]) - 1) >> tlog[a];
+    return c;
+}
+
+// The candidate that pads the box least (ties: the earlier candidate in the list).
+static void default_tlog(const int n[3], int out[3]) {
+    long long best = -1;
+    for (int s = 0; s < kNumShapes; s++) {
+        const long long cells = tile_count(n, kShapes[s]) * kTileThreads;
+        if (best < 0 || cells < best) {
+            best = cells;
+            for (int a = 0; a < 3; a++) out[a] = kShapes[s][a];
+        }
+    }
+}
+
+static void append_tiles(const int n[3], const int tlog[3], int box_index, std::vector<Tile>& out) {
+    const int ti = 1 << tlog[0], tj = 1 << tlog[1], tk = 1 << tlog[2];
+    for (int i0 = 0; i0 < n[0]; i0 += ti)
+        for (int j0 = 0; j0 < n[1]; j0 += tj)
+            for (int k0 = 0; k0 < n[2]; k0 += tk) out.push_back(Tile{box_index, i0, j0, k0});
+}
+
 static Geometry geometry(const cns_box_desc* d) {
     Geometry g;
-    int ti, tj, tk;
-    tile_shape(&ti, &tj, &tk);
     const long long g0 = d->n[0] + 2 * CNS_NG, g1 = d->n[1] + 2 * CNS_NG, g2 = d->n[2] + 2 * CNS_NG;
     g.pk = (int)((g2 + 7) / 8 * 8);
     g.sj = g.pk;
     g.si = g1 * g.sj;
     g.fs = g0 * g.si;
     const size_t esz = d->precision == CNS_MIXED ? 4 : 8;
-    g.ntiles = ((d->n[0] + ti - 1) / ti) * ((d->n[1] + tj - 1) / tj) * ((d->n[2] + tk - 1) / tk);
+    g.ntiles = 0;  // capacity: the largest tile count over the candidate shapes
+    for (int sh = 0; sh < kNumShapes; sh++) g.ntiles = std::max<long long>(g.ntiles, tile_count(d->n, kShapes[sh]));
     size_t o = 0;
     g.off_sc = o;      o = align256(o + sizeof(BoxScalars));
     g.off_dtlog = o;   o = align256(o + sizeof(double) * DTLOG_CAP);
@@ -179,6 +210,7 @@ struct cns_box {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     bool primed = false;
+    int ntiles = 0;  // tiles of the current shape (view.tlog)
     cudaGraphExec_t gexec = nullptr;
     cns_batch* batch = nullptr;
 };
@@ -230,13 +262,10 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     b->d_tiles = (Tile*)(b->arena + g.off_tiles);
     b->d_aos = (double*)(b->arena + g.off_aos);
     b->d_sc = v.sc;
-    int ti, tj, tk;
-    tile_shape(&ti, &tj, &tk);
+    default_tlog(desc->n, v.tlog);
     std::vector<Tile> tiles;
-    tiles.reserve(g.ntiles);
-    for (int i0 = 0; i0 < desc->n[0]; i0 += ti)
-        for (int j0 = 0; j0 < desc->n[1]; j0 += tj)
-            for (int k0 = 0; k0 < desc->n[2]; k0 += tk) tiles.push_back(Tile{0, i0, j0, k0});
+    append_tiles(desc->n, v.tlog, 0, tiles);
+    b->ntiles = (int)tiles.size();
     e = cudaMemsetAsync(b->arena, 0, g.total, b->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_view, &v, sizeof v, cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess)
@@ -302,7 +331,7 @@ static int prime(cns_box* b, const BoxScalars* restore = nullptr) {
         CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
         CK(launch_refs(b->d_view, 1, b->stream));
     }
-    CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->geo.ntiles, b->stream));
+    CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->ntiles, b->stream));
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return CNS_OK;
@@ -391,9 +420,9 @@ static int enqueue_step(const BoxView* views, int nviews, const Tile* t64, int n
 
 static int box_tiles(const cns_box* b, const Tile** t64, int* n64, const Tile** t32, int* n32) {
     if (b->desc.precision == CNS_MIXED) {
-        *t64 = nullptr, *n64 = 0, *t32 = b->d_tiles, *n32 = b->geo.ntiles;
+        *t64 = nullptr, *n64 = 0, *t32 = b->d_tiles, *n32 = b->ntiles;
     } else {
-        *t64 = b->d_tiles, *n64 = b->geo.ntiles, *t32 = nullptr, *n32 = 0;
+        *t64 = b->d_tiles, *n64 = b->ntiles, *t32 = nullptr, *n32 = 0;
     }
     return CNS_OK;
 }
@@ -517,13 +546,25 @@ struct cns_batch {
     BoxView* d_views = nullptr;
     Tile* d_tiles = nullptr;
     size_t cap_views = 0, cap_tiles = 0;
-    int n64 = 0, n32 = 0;
+    int n64 = 0, n32 = 0, nviews = 0;
     cudaStream_t stream = nullptr, own_stream = nullptr;
     bool dirty = true;
     cudaGraphExec_t gexec = nullptr;
 };
 
 static cudaStream_t batch_stream(cns_batch* bt) { return bt->stream; }
+
+// Make `later` wait for everything queued on `earlier` so far (no host blocking).
+static int order_after(cudaStream_t later, cudaStream_t earlier) {
+    if (later == earlier) return CNS_OK;
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, earlier);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(later, ev, 0);
+    cudaEventDestroy(ev);
+    if (e != cudaSuccess) return fail_cuda(e, "order_after", __LINE__);
+    return CNS_OK;
+}
 
 extern "C" int cns_batch_create(cns_batch** out) {
     if (!out) return fail(CNS_ERR_INVALID, "null output handle");
@@ -564,6 +605,9 @@ extern "C" int cns_batch_add(cns_batch* bt, cns_box* b) {
     if (b->batch) return fail(CNS_ERR_INVALID, "box already belongs to a batch");
     if (b->dev != bt->dev) return fail(CNS_ERR_INVALID, "box and batch live on different devices");
     if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
+    // work queued on the box's stream (an asynchronous init or upload) precedes the batch's
+    int rc = order_after(bt->stream, b->stream);
+    if (rc) return rc;
     bt->members.push_back(b);
     b->batch = bt;
     bt->dirty = true;
@@ -574,6 +618,9 @@ extern "C" int cns_batch_remove(cns_batch* bt, cns_box* b) {
     if (!bt || !b) return fail(CNS_ERR_INVALID, "null argument");
     auto it = std::find(bt->members.begin(), bt->members.end(), b);
     if (it == bt->members.end()) return fail(CNS_ERR_INVALID, "box is not in this batch");
+    // later work on the box's own stream (download, free) follows the batch's queued steps
+    int rc = order_after(b->stream, bt->stream);
+    if (rc) return rc;
     bt->members.erase(it);
     b->batch = nullptr;
     bt->dirty = true;
@@ -582,19 +629,14 @@ extern "C" int cns_batch_remove(cns_batch* bt, cns_box* b) {
 
 extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->members.size() : 0; }
 
-static int batch_rebuild(cns_batch* bt) {
+static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
     std::vector<Tile> tiles64, tiles32;
-    int ti, tj, tk;
-    tile_shape(&ti, &tj, &tk);
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
-        auto& dst = b->desc.precision == CNS_MIXED ? tiles32 : tiles64;
-        for (int i0 = 0; i0 < b->desc.n[0]; i0 += ti)
-            for (int j0 = 0; j0 < b->desc.n[1]; j0 += tj)
-                for (int k0 = 0; k0 < b->desc.n[2]; k0 += tk) dst.push_back(Tile{(int)m, i0, j0, k0});
+        append_tiles(b->desc.n, b->view.tlog, (int)m, b->desc.precision == CNS_MIXED ? tiles32 : tiles64);
     }
     const size_t nt = tiles64.size() + tiles32.size();
     if (views.size() > bt->cap_views) {
@@ -615,9 +657,14 @@ static int batch_rebuild(cns_batch* bt) {
         CK(cudaMemcpy(bt->d_tiles + tiles64.size(), tiles32.data(), sizeof(Tile) * tiles32.size(), cudaMemcpyHostToDevice));
     bt->n64 = (int)tiles64.size();
     bt->n32 = (int)tiles32.size();
+    bt->nviews = (int)views.size();
     if (bt->gexec) {
         cudaGraphExecDestroy(bt->gexec);
         bt->gexec = nullptr;
+    }
+    if (!capture) {
+        bt->dirty = true;  // tables are current, the graph is not
+        return CNS_OK;
     }
     if (!views.empty()) {
         int rc = capture_step(bt->own_stream, &bt->gexec, bt->d_views, (int)views.size(), bt->d_tiles, bt->n64,
@@ -982,5 +1029,145 @@ extern "C" int cns_box_load(cns_box* b, const char* path) {
     int rc = prime(b, &s);
     if (rc) return rc;
     CK(cudaStreamSynchronize(b->stream));
+    return CNS_OK;
+}
+
+
+// ---- tile shapes and the autotuner ---------------------------------------------------------
+static int valid_tlog(const int t[3]) {
+    for (int a = 0; a < 3; a++)
+        if (t[a] < 0 || t[a] > 8) return 0;
+    return t[0] + t[1] + t[2] == 8 && t[2] >= 3;
+}
+
+extern "C" int cns_box_get_tile(const cns_box* b, int tlog[3]) {
+    if (!b || !tlog) return fail(CNS_ERR_INVALID, "null argument");
+    for (int a = 0; a < 3; a++) tlog[a] = b->view.tlog[a];
+    return CNS_OK;
+}
+
+// Apply a tile shape to a box's own work list and device view (the batch, if any, is rebuilt
+// lazily).  Results do not depend on the shape: every cell's arithmetic is the same.
+static int apply_tile(cns_box* b, const int tlog[3]) {
+    if (!valid_tlog(tlog)) return fail(CNS_ERR_INVALID, "tile shape: log2 extents in [0,8] summing to 8, k >= 3");
+    if (tile_count(b->desc.n, tlog) > b->geo.ntiles) return fail(CNS_ERR_CAPACITY, "tile shape has too many tiles");
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
+    for (int a = 0; a < 3; a++) b->view.tlog[a] = tlog[a];
+    std::vector<Tile> tiles;
+    append_tiles(b->desc.n, tlog, 0, tiles);
+    b->ntiles = (int)tiles.size();
+    CK(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_view, &b->view, sizeof(BoxView), cudaMemcpyHostToDevice));
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    if (b->batch) b->batch->dirty = true;
+    return CNS_OK;
+}
+
+extern "C" int cns_box_set_tile(cns_box* b, const int tlog[3]) {
+    if (!b || !tlog) return fail(CNS_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(b->dev));
+    return apply_tile(b, tlog);
+}
+
+// Keep a copy of the state (device AoS staging) and the scalars, and put them back: trial
+// steps of the autotuner leave no trace, and the run continues bit for bit.
+static int save_state(cns_box* b, BoxScalars* hs) {
+    CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
+    return read_scalars(b, hs);
+}
+static int restore_state(cns_box* b, const BoxScalars* hs) {
+    CK(op_aos_to_box(b->d_aos, b->view, b->stream));
+    return prime(b, hs);
+}
+
+extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], double* best_ms) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
+    if (b->batch) return fail(CNS_ERR_INVALID, "autotune the batch this box belongs to");
+    if (trial_steps < 1) trial_steps = 1;
+    CK(cudaSetDevice(b->dev));
+    BoxScalars hs;
+    int rc = save_state(b, &hs);
+    if (rc) return rc;
+    int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]};
+    double best_t = 1e300;
+    for (int s = -1; s < kNumShapes; s++) {  // s = -1: a warm-up trial, not scored
+        const int* t = kShapes[s < 0 ? 0 : s];
+        if ((rc = apply_tile(b, t))) return rc;
+        const Tile *t64, *t32;
+        int n64, n32;
+        box_tiles(b, &t64, &n64, &t32, &n32);
+        double ms = 0.0;
+        if ((rc = timed_run(b->stream, trial_steps, b->d_view, 1, t64, n64, t32, n32, nullptr, nullptr, &ms))) return rc;
+        if ((rc = restore_state(b, &hs))) return rc;
+        if (s >= 0 && ms < best_t) {
+            best_t = ms;
+            for (int a = 0; a < 3; a++) best[a] = t[a];
+        }
+    }
+    if ((rc = apply_tile(b, best))) return rc;
+    if ((rc = restore_state(b, &hs))) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (tlog_out)
+        for (int a = 0; a < 3; a++) tlog_out[a] = best[a];
+    if (best_ms) *best_ms = best_t / trial_steps;
+    return CNS_OK;
+}
+
+// Policies: 0 = every member on its least-padding shape; 1 + s = every member on kShapes[s].
+static int apply_policy(cns_batch* bt, int policy) {
+    for (auto* b : bt->members) {
+        int t[3];
+        if (policy == 0)
+            default_tlog(b->desc.n, t);
+        else
+            for (int a = 0; a < 3; a++) t[a] = kShapes[policy - 1][a];
+        int rc = apply_tile(b, t);
+        if (rc) return rc;
+    }
+    return batch_rebuild(bt, false);
+}
+
+extern "C" int cns_batch_autotune(cns_batch* bt, int trial_steps, int* chosen_policy, double* best_ms) {
+    if (!bt) return fail(CNS_ERR_INVALID, "null batch");
+    if (bt->members.empty()) return CNS_OK;
+    if (trial_steps < 1) trial_steps = 1;
+    CK(cudaSetDevice(bt->dev));
+    CK(cudaStreamSynchronize(bt->stream));
+    std::vector<BoxScalars> saved(bt->members.size());
+    int rc;
+    for (size_t m = 0; m < bt->members.size(); m++)
+        if ((rc = save_state(bt->members[m], &saved[m]))) return rc;
+    auto restore_all = [&]() -> int {
+        for (size_t m = 0; m < bt->members.size(); m++) {
+            int r = restore_state(bt->members[m], &saved[m]);
+            if (r) return r;
+            CK(cudaStreamSynchronize(bt->members[m]->stream));
+        }
+        return CNS_OK;
+    };
+    int best = 0;
+    double best_t = 1e300;
+    for (int policy = -1; policy <= kNumShapes; policy++) {  // -1: warm-up with policy 0
+        if ((rc = apply_policy(bt, policy < 0 ? 0 : policy))) return rc;
+        double ms = 0.0;
+        rc = timed_run(bt->stream, trial_steps, bt->d_views, bt->nviews, bt->d_tiles, bt->n64, bt->d_tiles + bt->n64,
+                       bt->n32, nullptr, nullptr, &ms);
+        if (rc) return rc;
+        if ((rc = restore_all())) return rc;
+        if (policy >= 0 && ms < best_t) {
+            best_t = ms;
+            best = policy;
+        }
+    }
+    if ((rc = apply_policy(bt, best))) return rc;
+    if ((rc = restore_all())) return rc;
+    if ((rc = batch_rebuild(bt, true))) return rc;
+    if (chosen_policy) *chosen_policy = best;
+    if (best_ms) *best_ms = best_t / trial_steps;
     return CNS_OK;
 }

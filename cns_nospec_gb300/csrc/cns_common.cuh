@@ -3,7 +3,7 @@
 // Device layout of one periodic box (n0 x n1 x n2 interior cells, NG = 4 ghost cells a side):
 // structure of arrays, one field after another; inside a field the reference's spatial order
 // (i slowest, k fastest, cpu/helper_functions.cpp:100-122) with each k row padded to `pk`
-// elements (a multiple of 32, so every row starts on a 128-byte boundary for FP32 and FP64).
+// elements (a multiple of 8: 64-byte rows for FP64, 32-byte for FP32; TMA-legal strides).
 //   elem(f, i, j, k) = f*fs + i*si + j*sj + k      (i, j, k ghost-inclusive, 0..n+7)
 // i pairs with dx[0], j with dx[1], k with dx[2], exactly as in the reference.
 #pragma once
@@ -95,15 +95,26 @@ struct BoxView {
     double* dtlog;          // dt of completed steps, ring of DTLOG_CAP entries
     double cfl;
     int precision;          // 0 = plain FP64, 1 = mixed
-    int pad;
+    int tlog[3];            // tile shape of this box: log2 of its (i, j, k) extent; the three sum to 8
+                            // (256 threads, one cell each, k fastest across a warp)
     CoefT<double> c64;
     CoefT<float> c32;
 };
 
-// A unit of work: one tile of one box.  Tiles are TI x TJ x TK cells with origin (i0,j0,k0).
+// A unit of work: one tile of one box, with origin (i0, j0, k0); its shape is the box's tlog.
 struct Tile {
     int box, i0, j0, k0;
 };
+
+constexpr int kTileThreads = 256;
+
+// The cell of this thread inside a tile of shape tlog (k fastest, then j, then i).
+__device__ __forceinline__ void tile_cell(const int tlog[3], int t, int* ti, int* tj, int* tk) {
+    const int lk = tlog[2], lj = tlog[1];
+    *tk = t & ((1 << lk) - 1);
+    *tj = (t >> lk) & ((1 << lj) - 1);
+    *ti = t >> (lk + lj);
+}
 
 __host__ __device__ inline long long cell_off(const BoxView& b, int i, int j, int k) {
     // (i, j, k) interior indices, 0-based; returns the element offset inside one field

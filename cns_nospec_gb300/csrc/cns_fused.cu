@@ -1,7 +1,8 @@
 // cns_fused.cu -- persistent tile-walking kernels for the RK3 stages (see cns_fused.cuh).
 //
 // Every kernel walks a work list of tiles (box, i0, j0, k0); one launch covers every box of a
-// batch.  A tile is TI x TJ x TK cells (k = unit stride), one cell per thread.
+// batch.  A tile is 256 cells, one per thread, in the shape its box carries (tlog), so boxes
+// with different tile shapes share a launch.
 #include "cns_fused.cuh"
 #include "cns_internal.h"
 
@@ -11,13 +12,14 @@ template <class R>
 __device__ __forceinline__ R ld(const R* p) { return __ldg(p); }
 
 // ---- k_prim: primitives + flux functions + Courant of the uploaded state -------------------
-template <class R, int TI, int TJ, int TK>
-__global__ void __launch_bounds__(TI* TJ* TK) k_prim(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
+template <class R>
+__global__ void __launch_bounds__(kTileThreads) k_prim(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
                                                      int ntiles) {
-    const int tk = threadIdx.x % TK, tj = (threadIdx.x / TK) % TJ, ti = threadIdx.x / (TK * TJ);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
+        int ti, tj, tk;
+        tile_cell(b.tlog, threadIdx.x, &ti, &tj, &tk);
         const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
         double cour = 0.0;
         int health = 0;
@@ -35,13 +37,14 @@ __global__ void __launch_bounds__(TI* TJ* TK) k_prim(const BoxView* __restrict__
 }
 
 // ---- k_deriv: first derivatives of (u,v,w) -> mixed-term sums and viscous dissipation -------
-template <class R, int TI, int TJ, int TK>
-__global__ void __launch_bounds__(TI* TJ* TK) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
+template <class R>
+__global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
                                                       int ntiles, int stage) {
-    const int tk = threadIdx.x % TK, tj = (threadIdx.x / TK) % TJ, ti = threadIdx.x / (TK * TJ);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
+        int ti, tj, tk;
+        tile_cell(b.tlog, threadIdx.x, &ti, &tj, &tk);
         const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
         if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
         const int pr = b.sc->pbase ^ ((stage - 1) & 1);
@@ -74,13 +77,14 @@ __global__ void __launch_bounds__(TI* TJ* TK) k_deriv(const BoxView* __restrict_
 }
 
 // ---- k_assemble: D + F, RK stage combine, fused ctoprim/flux/ghost write-back -------------
-template <class R, int STAGE, int TI, int TJ, int TK>
-__global__ void __launch_bounds__(TI* TJ* TK) k_assemble(const BoxView* __restrict__ boxes,
+template <class R, int STAGE>
+__global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __restrict__ boxes,
                                                          const Tile* __restrict__ tiles, int ntiles) {
-    const int tk = threadIdx.x % TK, tj = (threadIdx.x / TK) % TJ, ti = threadIdx.x / (TK * TJ);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
+        int ti, tj, tk;
+        tile_cell(b.tlog, threadIdx.x, &ti, &tj, &tk);
         const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
         double cour = 0.0;
         int health = 0;
@@ -203,48 +207,40 @@ __global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int fli
 }
 
 // ---- launch helpers ---------------------------------------------------------------------
-constexpr int TI = 2, TJ = 4, TK = 32, NT = TI * TJ * TK;
-
 static int grid_for(const void* fn, int ntiles) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kTileThreads, 0);
     if (per < 1) per = 1;
     int g = nsm * per;
     return ntiles < g ? ntiles : g;
 }
 
-void tile_shape(int* ti, int* tj, int* tk) {
-    *ti = TI;
-    *tj = TJ;
-    *tk = TK;
-}
-
 template <class R>
 static cudaError_t launch_prim_t(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
-    auto fn = k_prim<R, TI, TJ, TK>;
-    fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+    auto fn = k_prim<R>;
+    fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
     return cudaGetLastError();
 }
 template <class R>
 static cudaError_t launch_deriv_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
-    auto fn = k_deriv<R, TI, TJ, TK>;
-    fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles, stage);
+    auto fn = k_deriv<R>;
+    fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles, stage);
     return cudaGetLastError();
 }
 template <class R>
 static cudaError_t launch_assemble_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (stage == 1) {
-        auto fn = k_assemble<R, 1, TI, TJ, TK>;
-        fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+        auto fn = k_assemble<R, 1>;
+        fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
     } else if (stage == 2) {
-        auto fn = k_assemble<R, 2, TI, TJ, TK>;
-        fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+        auto fn = k_assemble<R, 2>;
+        fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
     } else {
-        auto fn = k_assemble<R, 3, TI, TJ, TK>;
-        fn<<<grid_for((const void*)fn, ntiles), NT, 0, st>>>(boxes, tiles, ntiles);
+        auto fn = k_assemble<R, 3>;
+        fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
     }
     return cudaGetLastError();
 }

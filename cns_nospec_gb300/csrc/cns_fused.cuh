@@ -179,13 +179,16 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
     store_img(Pw + PHU * fs, b, c, i, j, k, dH * u, 1);
     store_img(Pw + PHV * fs, b, c, i, j, k, dH * v, 2);
     store_img(Pw + PHW * fs, b, c, i, j, k, dH * w, 4);
-    const float p = (float)(pd + sc.p_ref);
     if (!want_cour) return 0.0;
-    const float cs = sqrtf(((float)kGamma * p) * rf);
-    const float cx = (cs + fabsf(u)) * b.c32.cour[0];
-    const float cy = (cs + fabsf(v)) * b.c32.cour[1];
-    const float cz = (cs + fabsf(w)) * b.c32.cour[2];
-    return (double)fmaxf(fmaxf(cx, cy), cz);
+    // The Courant number sets dt, and an FP32 dt would advance the mixed form by a different
+    // time each step (a drift of ~1e-7 dt per step that dominates its error against FP64).
+    // Formed in FP64 once per step: 1/rho by one Newton step from the FP32 seed (~1e-14).
+    const double rinv = fma(r64, fma(-rho, r64, 1.0), r64);
+    const double cs = sqrt((kGamma * (pd + sc.p_ref)) * rinv);
+    const double cx = (cs + fabs(un[1]) * rinv) * b.c64.cour[0];
+    const double cy = (cs + fabs(un[2]) * rinv) * b.c64.cour[1];
+    const double cz = (cs + fabs(un[3]) * rinv) * b.c64.cour[2];
+    return fmax(fmax(cx, cy), cz);
 }
 
 // Warp max of positive doubles via their bit patterns; lane 0 folds it into the box max.

@@ -9,7 +9,6 @@ namespace cns {
 int set_error(int code, const char* msg);
 
 // fused RK3 stage kernels (cns_fused.cu); precision 0 = FP64 stencils, 1 = FP32 stencils
-void tile_shape(int* ti, int* tj, int* tk);
 cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st);
 cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
                          cudaStream_t st);

@@ -189,6 +189,21 @@ class Box:
         L.check(self.lib.cns_box_last_dt(self.h, C.byref(dt), C.byref(n)))
         return dt.value, n.value
 
+    def tile(self):
+        t = (C.c_int * 3)()
+        L.check(self.lib.cns_box_get_tile(self.h, t))
+        return tuple(t)
+
+    def set_tile(self, tlog):
+        L.check(self.lib.cns_box_set_tile(self.h, (C.c_int * 3)(*tlog)))
+
+    def autotune(self, trial_steps=2):
+        """Pick the fastest tile shape by timing trial steps (state restored afterwards)."""
+        t = (C.c_int * 3)()
+        ms = C.c_double()
+        L.check(self.lib.cns_box_autotune(self.h, int(trial_steps), t, C.byref(ms)))
+        return tuple(t), ms.value
+
     def launches_per_step(self) -> int:
         return int(self.lib.cns_box_launches_per_step(self.h))
 
@@ -229,6 +244,14 @@ class Batch:
 
     def sync(self):
         L.check(self.lib.cns_batch_sync(self.h))
+
+    def autotune(self, trial_steps=2):
+        """Time each tile-shape policy on the members (states restored) and keep the fastest;
+        returns (policy, ms per step): policy 0 = per-box least padding, 1+s = candidate s."""
+        pol = C.c_int()
+        ms = C.c_double()
+        L.check(self.lib.cns_batch_autotune(self.h, int(trial_steps), C.byref(pol), C.byref(ms)))
+        return pol.value, ms.value
 
     def close(self):
         if self.h:

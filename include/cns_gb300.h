@@ -192,6 +192,20 @@ int cns_batch_size(const cns_batch *batch);
 int cns_batch_advance(cns_batch *batch, int nsteps);
 int cns_batch_sync(cns_batch *batch);
 
+/* ---- tile shapes and the autotuner -------------------------------------------------------
+ * Work is cut into tiles of 256 cells (one per thread, k fastest across a warp); a box's tile
+ * shape is tlog[3] = log2 of the tile's (i, j, k) extents, summing to 8 with tlog[2] >= 3.
+ * The shape changes only speed, never results: every cell's arithmetic is the same.
+ * A new box starts on the candidate shape that pads it least. */
+int cns_box_get_tile(const cns_box *box, int tlog[3]);
+int cns_box_set_tile(cns_box *box, const int tlog[3]);
+/* Time trial_steps RK3 steps of the box on every candidate shape and keep the fastest; the
+ * box's state is restored afterwards, so the run continues bit for bit.  Blocks. */
+int cns_box_autotune(cns_box *box, int trial_steps, int tlog_out[3], double *best_ms_per_step);
+/* Same for a batch: policy 0 = every member on its least-padding shape, 1 + s = every member
+ * on candidate shape s; the fastest policy is kept and the graph re-captured. */
+int cns_batch_autotune(cns_batch *batch, int trial_steps, int *chosen_policy, double *best_ms_per_step);
+
 #ifdef __cplusplus
 }
 #endif

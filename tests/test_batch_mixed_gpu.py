@@ -100,3 +100,55 @@ def test_mixed_128cube_100_steps_vs_fp64(gpu, cns):
         b.close()
     err = normwise(out[cns.CNS_MIXED], out[cns.CNS_FP64])
     assert err.max() <= MIXED_TOL, err
+
+
+def test_every_tile_shape_gives_identical_bits(gpu, cns):
+    n = (19, 23, 37)
+    U0 = I.initial_state(n, perturb=1e-3, seed=13)
+    ref = None
+    shapes = [(1, 2, 5), (0, 3, 5), (0, 2, 6), (2, 2, 4), (2, 3, 3), (3, 2, 3), (1, 4, 3)]
+    for prec in (0, 1):
+        ref = None
+        for t in shapes:
+            b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
+            b.set_tile(t)
+            assert b.tile() == t
+            b.upload(U0)
+            b.advance(3)
+            out = b.download()
+            b.close()
+            if ref is None:
+                ref = out
+            assert np.array_equal(out, ref), (prec, t)
+    b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    for bad in [(1, 2, 2), (4, 4, 0), (0, 0, 9), (3, 3, 2)]:
+        with pytest.raises(cns.CnsError):
+            b.set_tile(bad)
+
+
+def test_autotune_keeps_results_and_state(gpu, cns):
+    """Autotuning runs trial steps, then restores every member: results equal the untuned run."""
+    mix = _boxes(cns, SPECS)
+    batch = cns.Batch()
+    for b, *_ in mix:
+        batch.add(b)
+    batch.advance(2)
+    pol, ms = batch.autotune(trial_steps=1)
+    assert 0 <= pol <= 12 and ms > 0
+    batch.advance(3)
+    batch.sync()
+    alone = _boxes(cns, SPECS)
+    for (bm, *_), (ba, *_r) in zip(mix, alone):
+        ba.advance(5)
+        assert np.array_equal(ba.download(), bm.download())
+        assert bm.last_dt()[1] == 5
+    batch.close()
+    box = cns.Box(24, I.box_dx(24), I.CFL, I.ETA, I.ALAM)
+    box.upload(I.initial_state(24, perturb=1e-3, seed=3))
+    t, ms = box.autotune(trial_steps=1)
+    assert sum(t) == 8 and ms > 0
+    box.advance(2)
+    other = cns.Box(24, I.box_dx(24), I.CFL, I.ETA, I.ALAM)
+    other.upload(I.initial_state(24, perturb=1e-3, seed=3))
+    other.advance(2)
+    assert np.array_equal(box.download(), other.download())
