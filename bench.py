@@ -241,7 +241,7 @@ def run_ours(args, dist):
     # ---- device-resident FP64 plain form: the headline value --------------------------------
     box = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_FP64)
     box.upload(U0)
-    tile64, _ = box.autotune(trial_steps=2)  # state restored afterwards
+    tile64, _, _ = box.autotune(trial_steps=2)  # state restored afterwards
     box.advance_timed(args.warmup)
     lib.cns_device_synchronize()
     dist.barrier()
@@ -260,7 +260,7 @@ def run_ours(args, dist):
     # ---- mixed form on the same box ----------------------------------------------------------
     mbox = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_MIXED)
     mbox.upload(U0)
-    tile32, _ = mbox.autotune(trial_steps=2)
+    tile32, kern32, _ = mbox.autotune(trial_steps=2)
     mbox.advance_timed(args.warmup)
     mms, _, mtotal = mbox.advance_timed(args.steps)
     mbox.sync()
@@ -324,7 +324,8 @@ def run_ours(args, dist):
         "config": {"workload": f"periodic box {n}^3 + 4 ghosts, FP64 plain RK3 (config 1 field, seed 1)",
                    "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
                    "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
-                   "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)}},
+                   "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)},
+                   "mixed_assembly_kernel": "tma" if kern32 == C.CNS_ASSEMBLE_TMA else "direct"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "api": "cns_new_advance (host U, copy in + 1 step + copy out)",
                 "pinned_host": pinned, "steps": k_e2e},

@@ -16,6 +16,7 @@ _VP = C.c_void_p
 
 CNS_OK, CNS_ERR_INVALID, CNS_ERR_NOMEM, CNS_ERR_NONFINITE, CNS_ERR_CUDA, CNS_ERR_CAPACITY, CNS_ERR_NODEVICE = range(7)
 CNS_FP64, CNS_MIXED = 0, 1
+CNS_ASSEMBLE_DIRECT, CNS_ASSEMBLE_TMA = 0, 1
 KERN_DERIV, KERN_ASSEMBLE, KERN_STEPEND, KERN_PRIM, KERN_COUNT = range(5)
 KERNEL_NAMES = ("k_deriv", "k_assemble", "k_stepend", "k_prim")
 
@@ -90,7 +91,9 @@ SIGNATURES = {
     "cns_batch_sync": (C.c_int, [_VP]),
     "cns_box_get_tile": (C.c_int, [_VP, _I]),
     "cns_box_set_tile": (C.c_int, [_VP, _I]),
-    "cns_box_autotune": (C.c_int, [_VP, C.c_int, _I, _D]),
+    "cns_box_autotune": (C.c_int, [_VP, C.c_int, _I, _I, _D]),
+    "cns_box_get_kernel": (C.c_int, [_VP, _I]),
+    "cns_box_set_kernel": (C.c_int, [_VP, C.c_int]),
     "cns_batch_autotune": (C.c_int, [_VP, C.c_int, _I, _D]),
 }
 

@@ -83,7 +83,9 @@ struct Geometry {
     int pk;
     long long sj, si, fs;
     size_t off_sc, off_dtlog, off_U, off_Us, off_P0, off_P1, off_S, off_view, off_tiles, off_aos, total;
-    int ntiles;
+    size_t off_xtiles, off_maps;  // mixed boxes: TMA-assembly tiles and tensor maps
+    int ntiles;                   // capacity of the tile list (largest candidate shape)
+    int nxtiles;                  // TMA-assembly tiles (8 x 8 x 32 cells)
 };
 
 static int validate_desc(const cns_box_desc* d) {
@@ -152,8 +154,25 @@ static Geometry geometry(const cns_box_desc* d) {
     g.off_view = o;    o = align256(o + sizeof(BoxView));
     g.off_tiles = o;   o = align256(o + sizeof(Tile) * g.ntiles);
     g.off_aos = o;     o = align256(o + sizeof(double) * CNS_NC * g0 * g1 * g2);
+    int xi, xj, xk;
+    tma_tile_shape(&xi, &xj, &xk);
+    g.nxtiles = 0;
+    g.off_xtiles = g.off_maps = 0;
+    if (d->precision == CNS_MIXED) {
+        g.nxtiles = ((d->n[0] + xi - 1) / xi) * ((d->n[1] + xj - 1) / xj) * ((d->n[2] + xk - 1) / xk);
+        g.off_xtiles = o;  o = align256(o + sizeof(Tile) * g.nxtiles);
+        g.off_maps = o;    o = align256(o + tma_maps_bytes());
+    }
     g.total = o;
     return g;
+}
+
+static void append_xtiles(const int n[3], int box_index, std::vector<Tile>& out) {
+    int xi, xj, xk;
+    tma_tile_shape(&xi, &xj, &xk);
+    for (int i0 = 0; i0 < n[0]; i0 += xi)
+        for (int j0 = 0; j0 < n[1]; j0 += xj)
+            for (int k0 = 0; k0 < n[2]; k0 += xk) out.push_back(Tile{box_index, i0, j0, k0});
 }
 
 template <class R>
@@ -211,6 +230,9 @@ struct cns_box {
     cudaStream_t own_stream = nullptr;
     bool primed = false;
     int ntiles = 0;  // tiles of the current shape (view.tlog)
+    Tile* d_xtiles = nullptr;  // mixed boxes: tiles of the TMA assembly kernel
+    int nxtiles = 0;
+    int kernel = CNS_ASSEMBLE_DIRECT;  // which k_assemble a mixed box runs
     cudaGraphExec_t gexec = nullptr;
     cns_batch* batch = nullptr;
 };
@@ -266,10 +288,28 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     std::vector<Tile> tiles;
     append_tiles(desc->n, v.tlog, 0, tiles);
     b->ntiles = (int)tiles.size();
+    std::vector<Tile> xtiles;
+    std::vector<unsigned char> maps;
+    if (desc->precision == CNS_MIXED) {
+        // the TMA assembly needs the box's tensor maps; without a driver entry point for them
+        // the box stays on the direct kernel
+        b->d_xtiles = (Tile*)(b->arena + g.off_xtiles);
+        append_xtiles(desc->n, 0, xtiles);
+        b->nxtiles = (int)xtiles.size();
+        maps.resize(tma_maps_bytes());
+        if (tma_encode_maps(v, maps.data()) == cudaSuccess) {
+            v.tma = b->arena + g.off_maps;
+            b->kernel = CNS_ASSEMBLE_TMA;
+        }
+    }
     e = cudaMemsetAsync(b->arena, 0, g.total, b->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_view, &v, sizeof v, cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess && !xtiles.empty())
+        e = cudaMemcpyAsync(b->d_xtiles, xtiles.data(), sizeof(Tile) * xtiles.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess && v.tma)
+        e = cudaMemcpyAsync((void*)v.tma, maps.data(), maps.size(), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {
         cudaFreeAsync(b->arena, b->own_stream);
@@ -382,10 +422,23 @@ extern "C" int cns_box_download(cns_box* b, double* U_host) {
     return CNS_OK;
 }
 
-// One RK3 step of the boxes behind `views` (tiles split by stencil precision).  When `ev`
-// is given, an event is recorded after every launch and the launch's kind appended to `kinds`.
-static int enqueue_step(const BoxView* views, int nviews, const Tile* t64, int n64, const Tile* t32, int n32,
-                        cudaStream_t st, std::vector<cudaEvent_t>* ev, std::vector<int>* kinds) {
+// The tiles of one RK3 step, split by kernel: FP64 boxes, mixed boxes (their derivative pass
+// always, their assembly when on the direct kernel), and mixed boxes on the TMA assembly.
+struct WorkLists {
+    const Tile* d64 = nullptr;
+    int nd64 = 0;
+    const Tile* d32 = nullptr;
+    int nd32 = 0;
+    const Tile* a32 = nullptr;
+    int na32 = 0;
+    const Tile* x32 = nullptr;
+    int nx32 = 0;
+};
+
+// One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
+// every launch and the launch's kind appended to `kinds`.
+static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cudaStream_t st,
+                        std::vector<cudaEvent_t>* ev, std::vector<int>* kinds) {
     auto mark = [&](int kind) -> int {
         if (!ev) return CNS_OK;
         cudaEvent_t e;
@@ -397,20 +450,24 @@ static int enqueue_step(const BoxView* views, int nviews, const Tile* t64, int n
     };
     int rc;
     for (int stage = 1; stage <= 3; stage++) {
-        if (n64) {
-            CK(launch_deriv(0, views, t64, n64, stage, st));
+        if (w.nd64) {
+            CK(launch_deriv(0, views, w.d64, w.nd64, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
-        if (n32) {
-            CK(launch_deriv(1, views, t32, n32, stage, st));
+        if (w.nd32) {
+            CK(launch_deriv(1, views, w.d32, w.nd32, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
-        if (n64) {
-            CK(launch_assemble(0, views, t64, n64, stage, st));
+        if (w.nd64) {
+            CK(launch_assemble(0, views, w.d64, w.nd64, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
-        if (n32) {
-            CK(launch_assemble(1, views, t32, n32, stage, st));
+        if (w.na32) {
+            CK(launch_assemble(1, views, w.a32, w.na32, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
+        if (w.nx32) {
+            CK(launch_assemble_tma(views, w.x32, w.nx32, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
     }
@@ -418,20 +475,24 @@ static int enqueue_step(const BoxView* views, int nviews, const Tile* t64, int n
     return mark(CNS_KERN_STEPEND);
 }
 
-static int box_tiles(const cns_box* b, const Tile** t64, int* n64, const Tile** t32, int* n32) {
+static WorkLists box_lists(const cns_box* b) {
+    WorkLists w;
     if (b->desc.precision == CNS_MIXED) {
-        *t64 = nullptr, *n64 = 0, *t32 = b->d_tiles, *n32 = b->ntiles;
+        w.d32 = b->d_tiles, w.nd32 = b->ntiles;
+        if (b->kernel == CNS_ASSEMBLE_TMA)
+            w.x32 = b->d_xtiles, w.nx32 = b->nxtiles;
+        else
+            w.a32 = b->d_tiles, w.na32 = b->ntiles;
     } else {
-        *t64 = b->d_tiles, *n64 = b->ntiles, *t32 = nullptr, *n32 = 0;
+        w.d64 = b->d_tiles, w.nd64 = b->ntiles;
     }
-    return CNS_OK;
+    return w;
 }
 
-static int capture_step(cudaStream_t st, cudaGraphExec_t* out, const BoxView* views, int nviews, const Tile* t64,
-                        int n64, const Tile* t32, int n32) {
+static int capture_step(cudaStream_t st, cudaGraphExec_t* out, const BoxView* views, int nviews, const WorkLists& w) {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_step(views, nviews, t64, n64, t32, n32, st, nullptr, nullptr);
+    int rc = enqueue_step(views, nviews, w, st, nullptr, nullptr);
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (rc) {
         if (graph) cudaGraphDestroy(graph);
@@ -451,28 +512,25 @@ extern "C" int cns_box_advance(cns_box* b, int nsteps) {
     if (nsteps < 0) return fail(CNS_ERR_INVALID, "nsteps < 0");
     if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
     CK(cudaSetDevice(b->dev));
-    const Tile *t64, *t32;
-    int n64, n32;
-    box_tiles(b, &t64, &n64, &t32, &n32);
     if (!b->gexec) {
-        int rc = capture_step(b->own_stream, &b->gexec, b->d_view, 1, t64, n64, t32, n32);
+        int rc = capture_step(b->own_stream, &b->gexec, b->d_view, 1, box_lists(b));
         if (rc) return rc;
     }
     for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(b->gexec, b->stream));
     return CNS_OK;
 }
 
-static int timed_run(cudaStream_t st, int nsteps, const BoxView* views, int nviews, const Tile* t64, int n64,
-                     const Tile* t32, int n32, double* kernel_ms, int* kernel_launches, double* total_ms) {
+static int timed_run(cudaStream_t st, int nsteps, const BoxView* views, int nviews, const WorkLists& w,
+                     double* kernel_ms, int* kernel_launches, double* total_ms) {
     std::vector<cudaEvent_t> ev;
     std::vector<int> kinds;
-    ev.reserve(8 * nsteps + 1);
-    kinds.reserve(8 * nsteps + 1);
+    ev.reserve(16 * nsteps + 1);
+    kinds.reserve(16 * nsteps + 1);
     cudaEvent_t e0;
     CK(cudaEventCreate(&e0));
     CK(cudaEventRecord(e0, st));
     int rc = CNS_OK;
-    for (int s = 0; s < nsteps && rc == CNS_OK; s++) rc = enqueue_step(views, nviews, t64, n64, t32, n32, st, &ev, &kinds);
+    for (int s = 0; s < nsteps && rc == CNS_OK; s++) rc = enqueue_step(views, nviews, w, st, &ev, &kinds);
     cudaError_t e = cudaStreamSynchronize(st);
     if (rc == CNS_OK && e != cudaSuccess) rc = fail_cuda(e, "cudaStreamSynchronize", __LINE__);
     if (rc == CNS_OK) {
@@ -505,10 +563,7 @@ extern "C" int cns_box_advance_timed(cns_box* b, int nsteps, double* kernel_ms, 
     if (nsteps < 0) return fail(CNS_ERR_INVALID, "nsteps < 0");
     if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
     CK(cudaSetDevice(b->dev));
-    const Tile *t64, *t32;
-    int n64, n32;
-    box_tiles(b, &t64, &n64, &t32, &n32);
-    return timed_run(b->stream, nsteps, b->d_view, 1, t64, n64, t32, n32, kernel_ms, kernel_launches, total_ms);
+    return timed_run(b->stream, nsteps, b->d_view, 1, box_lists(b), kernel_ms, kernel_launches, total_ms);
 }
 
 static int read_scalars(cns_box* b, BoxScalars* hs) {
@@ -546,7 +601,8 @@ struct cns_batch {
     BoxView* d_views = nullptr;
     Tile* d_tiles = nullptr;
     size_t cap_views = 0, cap_tiles = 0;
-    int n64 = 0, n32 = 0, nviews = 0;
+    int nviews = 0;
+    WorkLists lists;  // into d_tiles
     cudaStream_t stream = nullptr, own_stream = nullptr;
     bool dirty = true;
     cudaGraphExec_t gexec = nullptr;
@@ -632,13 +688,24 @@ extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->member
 static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
-    std::vector<Tile> tiles64, tiles32;
+    std::vector<Tile> d64, d32, a32, x32;  // the four lists of WorkLists
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
-        append_tiles(b->desc.n, b->view.tlog, (int)m, b->desc.precision == CNS_MIXED ? tiles32 : tiles64);
+        if (b->desc.precision != CNS_MIXED) {
+            append_tiles(b->desc.n, b->view.tlog, (int)m, d64);
+            continue;
+        }
+        append_tiles(b->desc.n, b->view.tlog, (int)m, d32);
+        if (b->kernel == CNS_ASSEMBLE_TMA)
+            append_xtiles(b->desc.n, (int)m, x32);
+        else
+            append_tiles(b->desc.n, b->view.tlog, (int)m, a32);
     }
-    const size_t nt = tiles64.size() + tiles32.size();
+    std::vector<Tile> all;
+    all.reserve(d64.size() + d32.size() + a32.size() + x32.size());
+    for (auto* v : {&d64, &d32, &a32, &x32}) all.insert(all.end(), v->begin(), v->end());
+    const size_t nt = all.size();
     if (views.size() > bt->cap_views) {
         cudaFree(bt->d_views);
         bt->d_views = nullptr;
@@ -652,11 +719,14 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
         CK(cudaMalloc((void**)&bt->d_tiles, sizeof(Tile) * bt->cap_tiles));
     }
     if (!views.empty()) CK(cudaMemcpy(bt->d_views, views.data(), sizeof(BoxView) * views.size(), cudaMemcpyHostToDevice));
-    if (!tiles64.empty()) CK(cudaMemcpy(bt->d_tiles, tiles64.data(), sizeof(Tile) * tiles64.size(), cudaMemcpyHostToDevice));
-    if (!tiles32.empty())
-        CK(cudaMemcpy(bt->d_tiles + tiles64.size(), tiles32.data(), sizeof(Tile) * tiles32.size(), cudaMemcpyHostToDevice));
-    bt->n64 = (int)tiles64.size();
-    bt->n32 = (int)tiles32.size();
+    if (!all.empty()) CK(cudaMemcpy(bt->d_tiles, all.data(), sizeof(Tile) * all.size(), cudaMemcpyHostToDevice));
+    WorkLists& w = bt->lists;
+    w = WorkLists();
+    Tile* at = bt->d_tiles;
+    w.d64 = at, w.nd64 = (int)d64.size(), at += d64.size();
+    w.d32 = at, w.nd32 = (int)d32.size(), at += d32.size();
+    w.a32 = at, w.na32 = (int)a32.size(), at += a32.size();
+    w.x32 = at, w.nx32 = (int)x32.size();
     bt->nviews = (int)views.size();
     if (bt->gexec) {
         cudaGraphExecDestroy(bt->gexec);
@@ -667,8 +737,7 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
         return CNS_OK;
     }
     if (!views.empty()) {
-        int rc = capture_step(bt->own_stream, &bt->gexec, bt->d_views, (int)views.size(), bt->d_tiles, bt->n64,
-                              bt->d_tiles + bt->n64, bt->n32);
+        int rc = capture_step(bt->own_stream, &bt->gexec, bt->d_views, (int)views.size(), bt->lists);
         if (rc) return rc;
     }
     bt->dirty = false;
@@ -1084,7 +1153,35 @@ static int restore_state(cns_box* b, const BoxScalars* hs) {
     return prime(b, hs);
 }
 
-extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], double* best_ms) {
+static int apply_kernel(cns_box* b, int kernel) {
+    if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA) return fail(CNS_ERR_INVALID, "unknown kernel %d", kernel);
+    if (kernel == CNS_ASSEMBLE_TMA && (b->desc.precision != CNS_MIXED || !b->view.tma))
+        return fail(CNS_ERR_INVALID, "the TMA assembly serves mixed-precision boxes with tensor maps only");
+    if (kernel == b->kernel) return CNS_OK;
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
+    b->kernel = kernel;
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    if (b->batch) b->batch->dirty = true;
+    return CNS_OK;
+}
+
+extern "C" int cns_box_get_kernel(const cns_box* b, int* kernel) {
+    if (!b || !kernel) return fail(CNS_ERR_INVALID, "null argument");
+    *kernel = b->kernel;
+    return CNS_OK;
+}
+
+extern "C" int cns_box_set_kernel(cns_box* b, int kernel) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    CK(cudaSetDevice(b->dev));
+    return apply_kernel(b, kernel);
+}
+
+extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], int* kernel_out, double* best_ms) {
     if (!b) return fail(CNS_ERR_INVALID, "null box");
     if (!b->primed) return fail(CNS_ERR_INVALID, "box has no state (upload first)");
     if (b->batch) return fail(CNS_ERR_INVALID, "autotune the batch this box belongs to");
@@ -1093,41 +1190,46 @@ extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], do
     BoxScalars hs;
     int rc = save_state(b, &hs);
     if (rc) return rc;
-    int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]};
+    const int nkern = (b->desc.precision == CNS_MIXED && b->view.tma) ? 2 : 1;
+    int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]}, best_k = b->kernel;
     double best_t = 1e300;
-    for (int s = -1; s < kNumShapes; s++) {  // s = -1: a warm-up trial, not scored
-        const int* t = kShapes[s < 0 ? 0 : s];
-        if ((rc = apply_tile(b, t))) return rc;
-        const Tile *t64, *t32;
-        int n64, n32;
-        box_tiles(b, &t64, &n64, &t32, &n32);
+    for (int c = -1; c < nkern * kNumShapes; c++) {  // c = -1: a warm-up trial, not scored
+        const int* t = kShapes[c < 0 ? 0 : c % kNumShapes];
+        const int k = c < 0 ? b->kernel : c / kNumShapes;
+        if ((rc = apply_tile(b, t)) || (rc = apply_kernel(b, k))) return rc;
         double ms = 0.0;
-        if ((rc = timed_run(b->stream, trial_steps, b->d_view, 1, t64, n64, t32, n32, nullptr, nullptr, &ms))) return rc;
+        if ((rc = timed_run(b->stream, trial_steps, b->d_view, 1, box_lists(b), nullptr, nullptr, &ms))) return rc;
         if ((rc = restore_state(b, &hs))) return rc;
-        if (s >= 0 && ms < best_t) {
+        if (c >= 0 && ms < best_t) {
             best_t = ms;
-            for (int a = 0; a < 3; a++) best[a] = t[a];
+            best_k = k;
+            for (int q = 0; q < 3; q++) best[q] = t[q];
         }
     }
-    if ((rc = apply_tile(b, best))) return rc;
+    if ((rc = apply_tile(b, best)) || (rc = apply_kernel(b, best_k))) return rc;
     if ((rc = restore_state(b, &hs))) return rc;
     CK(cudaStreamSynchronize(b->stream));
     if (tlog_out)
-        for (int a = 0; a < 3; a++) tlog_out[a] = best[a];
+        for (int q = 0; q < 3; q++) tlog_out[q] = best[q];
+    if (kernel_out) *kernel_out = best_k;
     if (best_ms) *best_ms = best_t / trial_steps;
     return CNS_OK;
 }
 
-// Policies: 0 = every member on its least-padding shape; 1 + s = every member on kShapes[s].
+// Policy p = shape + (kNumShapes + 1) * kernel: shape 0 = every member on its least-padding
+// shape, 1 + s = every member on kShapes[s]; kernel = the assembly kernel of the mixed members
+// (0 direct, 1 TMA).
 static int apply_policy(cns_batch* bt, int policy) {
+    const int shape = policy % (kNumShapes + 1), kernel = policy / (kNumShapes + 1);
     for (auto* b : bt->members) {
         int t[3];
-        if (policy == 0)
+        if (shape == 0)
             default_tlog(b->desc.n, t);
         else
-            for (int a = 0; a < 3; a++) t[a] = kShapes[policy - 1][a];
+            for (int a = 0; a < 3; a++) t[a] = kShapes[shape - 1][a];
         int rc = apply_tile(b, t);
         if (rc) return rc;
+        if (b->desc.precision == CNS_MIXED && b->view.tma && (rc = apply_kernel(b, kernel))) return rc;
     }
     return batch_rebuild(bt, false);
 }
@@ -1150,13 +1252,15 @@ extern "C" int cns_batch_autotune(cns_batch* bt, int trial_steps, int* chosen_po
         }
         return CNS_OK;
     };
+    bool any_tma = false;
+    for (auto* b : bt->members) any_tma = any_tma || (b->desc.precision == CNS_MIXED && b->view.tma);
+    const int npolicies = (kNumShapes + 1) * (any_tma ? 2 : 1);
     int best = 0;
     double best_t = 1e300;
-    for (int policy = -1; policy <= kNumShapes; policy++) {  // -1: warm-up with policy 0
+    for (int policy = -1; policy < npolicies; policy++) {  // -1: warm-up with policy 0
         if ((rc = apply_policy(bt, policy < 0 ? 0 : policy))) return rc;
         double ms = 0.0;
-        rc = timed_run(bt->stream, trial_steps, bt->d_views, bt->nviews, bt->d_tiles, bt->n64, bt->d_tiles + bt->n64,
-                       bt->n32, nullptr, nullptr, &ms);
+        rc = timed_run(bt->stream, trial_steps, bt->d_views, bt->nviews, bt->lists, nullptr, nullptr, &ms);
         if (rc) return rc;
         if ((rc = restore_all())) return rc;
         if (policy >= 0 && ms < best_t) {

@@ -79,7 +79,8 @@ struct BoxScalars {
 
 constexpr int DTLOG_CAP = 1024;
 
-enum { HEALTH_OK = 0, HEALTH_NONPOS_RHO = 1, HEALTH_NONFINITE = 2, HEALTH_NONPOS_EINT = 4 };
+// HEALTH_TIMEOUT: a bounded wait inside a kernel gave up (the kernel returned early).
+enum { HEALTH_OK = 0, HEALTH_NONPOS_RHO = 1, HEALTH_NONFINITE = 2, HEALTH_NONPOS_EINT = 4, HEALTH_TIMEOUT = 8 };
 
 // Everything a kernel needs about one box.  Kept in device memory (one entry per box) so
 // that a batched launch can walk tiles of many boxes.
@@ -93,6 +94,7 @@ struct BoxView {
     void* S;                // NSF fields, precision R
     BoxScalars* sc;
     double* dtlog;          // dt of completed steps, ring of DTLOG_CAP entries
+    const void* tma;        // mixed boxes: device copy of the TMA tensor maps of P[0], P[1], S
     double cfl;
     int precision;          // 0 = plain FP64, 1 = mixed
     int tlog[3];            // tile shape of this box: log2 of its (i, j, k) extent; the three sum to 8

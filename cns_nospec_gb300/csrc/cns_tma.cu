@@ -1,0 +1,494 @@
+// cns_tma.cu -- k_assemble of the mixed form with its stencil tiles staged by TMA.
+//
+// Tile: 8 (i) x 8 (j) x 32 (k) cells; 256 threads = 32 (k) x 8 (j), each thread owns the 8
+// cells of its (j, k) column along i.  The 20 FP32 fields the assembly reads are brought into
+// shared memory one after another as 3-D boxes of the tile plus a 4-cell halo only along the
+// axes that field is differenced on (a full 40x16x16 box for u, v, w, T; 32x8x16 for an
+// x-only field; ...), by cp.async.bulk.tensor.4d (a 4-D tensor map over (k, j, i, field) of
+// the box's P or S set), double-buffered: the copy of field g+1 is in flight while field g is
+// consumed.  i-direction taps come from a 16-deep register column, j/k taps from shared
+// memory with compile-time offsets.  The arithmetic is done in exactly the order of the
+// direct-load kernel (cns_fused.cu), so both give the same bits.
+//
+// Every mbarrier wait is bounded (about one second of global time); on expiry the block sets
+// HEALTH_TIMEOUT in the box's status, waits (bounded again) for its own copies and returns.
+#include <cuda.h>
+
+#include "cns_fused.cuh"
+#include "cns_internal.h"
+
+namespace cns {
+
+constexpr int XI = 8, XJ = 8, XK = 32;
+
+// The boxes: halo axes -> extents (k, j, i).
+enum { BX_FULL = 0, BX_I, BX_J, BX_K, BX_IJ, BX_IK, BX_JK, BX_C, BX_COUNT };
+__host__ __device__ constexpr int box_k(int s) { return (s == BX_FULL || s == BX_K || s == BX_IK || s == BX_JK) ? XK + 8 : XK; }
+__host__ __device__ constexpr int box_j(int s) { return (s == BX_FULL || s == BX_J || s == BX_IJ || s == BX_JK) ? XJ + 8 : XJ; }
+__host__ __device__ constexpr int box_i(int s) { return (s == BX_FULL || s == BX_I || s == BX_IJ || s == BX_IK) ? XI + 8 : XI; }
+__host__ __device__ constexpr int box_elems(int s) { return box_k(s) * box_j(s) * box_i(s); }
+constexpr int kBufElems = box_elems(BX_FULL);  // 10240 floats, the largest box
+
+// Tensor maps of one mixed box: P sets (7 shapes each) and the S set (I, J, K, C boxes).
+struct TmaMaps {
+    CUtensorMap p[2][7];
+    CUtensorMap s[4];
+};
+static_assert(sizeof(CUtensorMap) == 128, "CUtensorMap is 128 bytes");
+
+// The 20 loads of a tile, in consumption order: (set 0 = P / 1 = S, field, box shape).
+struct Load {
+    unsigned char set, field, shape;
+};
+__constant__ Load kSched[20] = {{1, SPHI, BX_C},   {0, PT, BX_FULL}, {0, PU, BX_FULL},  {1, SX, BX_I},
+                                {0, PV, BX_FULL}, {1, SY, BX_J},    {0, PW, BX_FULL},  {1, SZ, BX_K},
+                                {0, PMX, BX_I},   {0, PMY, BX_J},   {0, PMZ, BX_K},    {0, PFUU, BX_I},
+                                {0, PFUV, BX_IJ}, {0, PFUW, BX_IK}, {0, PFVV, BX_J},   {0, PFVW, BX_JK},
+                                {0, PFWW, BX_K},  {0, PHU, BX_I},   {0, PHV, BX_J},    {0, PHW, BX_K}};
+constexpr int kLoads = 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for the phase with the given parity, giving up after ~1 s of global time.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
+__device__ __forceinline__ void tma_load(float* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Issue load number g of this block (tile g / 20, entry g % 20) into buffer g & 1.
+__device__ __forceinline__ void issue(const BoxView* boxes, const Tile* tiles, int tile, int entry, int flip,
+                                      float* buf, uint64_t* bar) {
+    const Tile T = tiles[tile];
+    const BoxView& b = boxes[T.box];
+    const TmaMaps* maps = (const TmaMaps*)b.tma;
+    const Load L = kSched[entry];
+    const CUtensorMap* map;
+    if (L.set == 0) {
+        map = &maps->p[b.sc->pbase ^ flip][L.shape];  // stage s reads P[pbase ^ ((s-1)&1)]
+    } else {
+        const int si = L.shape == BX_I ? 0 : L.shape == BX_J ? 1 : L.shape == BX_K ? 2 : 3;
+        map = &maps->s[si];
+    }
+    const int hk = box_k(L.shape) == XK ? 0 : 4, hj = box_j(L.shape) == XJ ? 0 : 4, hi = box_i(L.shape) == XI ? 0 : 4;
+    mbar_expect_tx(bar, (uint32_t)(box_elems(L.shape) * sizeof(float)));
+    tma_load(buf, map, T.k0 + CNS_NG - hk, T.j0 + CNS_NG - hj, T.i0 + CNS_NG - hi, L.field, bar);
+}
+
+// ---- per-field consumers (compile-time box extents) ----------------------------------------
+// Offsets below are in elements of the box in shared memory: (ii, jj, kk) -> (ii*BJ + jj)*BK + kk.
+template <int S>
+struct Bx {
+    static constexpr int K = box_k(S), J = box_j(S), I = box_i(S);
+    static constexpr int HK = K == XK ? 0 : 4, HJ = J == XJ ? 0 : 4, HI = I == XI ? 0 : 4;
+    __device__ static __forceinline__ int at(int ii, int jj, int kk) { return (ii * J + jj) * K + kk; }
+};
+
+// acc + sum_m a_m (p[+m s] - p[-m s]) on shared memory, offsets s in elements
+__device__ __forceinline__ float sd1acc(float acc, const float* p, int s, const float* a) {
+    acc = fmaf(a[0], p[s] - p[-s], acc);
+    acc = fmaf(a[1], p[2 * s] - p[-2 * s], acc);
+    acc = fmaf(a[2], p[3 * s] - p[-3 * s], acc);
+    acc = fmaf(a[3], p[4 * s] - p[-4 * s], acc);
+    return acc;
+}
+__device__ __forceinline__ float sd1(const float* p, int s, const float* a) {
+    float acc = a[0] * (p[s] - p[-s]);
+    acc = fmaf(a[1], p[2 * s] - p[-2 * s], acc);
+    acc = fmaf(a[2], p[3 * s] - p[-3 * s], acc);
+    acc = fmaf(a[3], p[4 * s] - p[-4 * s], acc);
+    return acc;
+}
+__device__ __forceinline__ float sd2acc(float acc, const float* p, int s, const float* b) {
+    acc = fmaf(b[0], p[s] + p[-s], acc);
+    acc = fmaf(b[1], p[2 * s] + p[-2 * s], acc);
+    acc = fmaf(b[2], p[3 * s] + p[-3 * s], acc);
+    acc = fmaf(b[3], p[4 * s] + p[-4 * s], acc);
+    return acc;
+}
+// the same on a register column (i direction), centre index c
+__device__ __forceinline__ float cd1acc(float acc, const float* col, int c, const float* a) {
+    acc = fmaf(a[0], col[c + 1] - col[c - 1], acc);
+    acc = fmaf(a[1], col[c + 2] - col[c - 2], acc);
+    acc = fmaf(a[2], col[c + 3] - col[c - 3], acc);
+    acc = fmaf(a[3], col[c + 4] - col[c - 4], acc);
+    return acc;
+}
+__device__ __forceinline__ float cd1(const float* col, int c, const float* a) {
+    float acc = a[0] * (col[c + 1] - col[c - 1]);
+    acc = fmaf(a[1], col[c + 2] - col[c - 2], acc);
+    acc = fmaf(a[2], col[c + 3] - col[c - 3], acc);
+    acc = fmaf(a[3], col[c + 4] - col[c - 4], acc);
+    return acc;
+}
+__device__ __forceinline__ float cd2acc(float acc, const float* col, int c, const float* b) {
+    acc = fmaf(b[0], col[c + 1] + col[c - 1], acc);
+    acc = fmaf(b[1], col[c + 2] + col[c - 2], acc);
+    acc = fmaf(b[2], col[c + 3] + col[c - 3], acc);
+    acc = fmaf(b[3], col[c + 4] + col[c - 4], acc);
+    return acc;
+}
+
+// The full-box (u, v, w or T) pass: centre weight, then the i, j, k second differences.
+__device__ __forceinline__ void lap_full(const float* s, int tj, int tk, float cw, const float* wi, const float* wj,
+                                         const float* wk, float* acc, float* ctr, bool init_from_acc) {
+    using B = Bx<BX_FULL>;
+    float col[16];
+#pragma unroll
+    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk + 4)];
+#pragma unroll
+    for (int i = 0; i < XI; i++) {
+        const float c0 = col[i + 4];
+        ctr[i] = c0;
+        float a = init_from_acc ? fmaf(cw, c0, acc[i]) : cw * c0;
+        a = cd2acc(a, col, i + 4, wi);
+        const float* p = s + B::at(i + 4, tj + 4, tk + 4);
+        a = sd2acc(a, p, B::K, wj);
+        a = sd2acc(a, p, 1, wk);
+        acc[i] = a;
+    }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView* __restrict__ boxes,
+                                                               const Tile* __restrict__ tiles, int ntiles) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* buf[2] = {(float*)smem_raw, (float*)smem_raw + kBufElems};
+    uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(float));
+    const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
+    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    if (my_tiles <= 0) return;
+    const int total = my_tiles * kLoads;
+    if (tid == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    constexpr int flip = (STAGE - 1) & 1;
+    if (tid == 0) issue(boxes, tiles, blockIdx.x, 0, flip, buf[0], &bar[0]);
+
+    float dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
+    int g = 0;
+    for (int it = 0; it < my_tiles; it++) {
+        const int tile = blockIdx.x + it * gridDim.x;
+        const Tile T = tiles[tile];
+        const BoxView& b = boxes[T.box];
+        const CoefT<float>& cf = b.c32;
+        for (int e = 0; e < kLoads; e++, g++) {
+            if (tid == 0 && g + 1 < total) {
+                const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
+                issue(boxes, tiles, nt, (g + 1) % kLoads, flip, buf[(g + 1) & 1], &bar[(g + 1) & 1]);
+            }
+            const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                    // let the copies this block started finish (bounded) before returning
+                    mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+                    if (g + 1 < total) mbar_wait_bounded(&bar[(g + 1) & 1], (uint32_t)(((g + 1) >> 1) & 1));
+                }
+                return;
+            }
+            const float* s = buf[g & 1];
+            switch (e) {
+                case 0: {  // SPHI: de starts from eta * Phi
+                    using B = Bx<BX_C>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) de[i] = s[B::at(i, tj, tk)];
+                    break;
+                }
+                case 1: {  // PT: de = tc T0 + phi, then the x, y, z second differences
+                    float t0[XI];
+                    lap_full(s, tj, tk, cf.tc, cf.tl[0], cf.tl[1], cf.tl[2], de, t0, true);
+                    break;
+                }
+                case 2:  // PU: dmx = vc0 u0 + x, y, z second differences
+                    lap_full(s, tj, tk, cf.vc[0], cf.vl[0][0], cf.vl[0][1], cf.vl[0][2], dmx, c0, false);
+                    break;
+                case 3: {  // SX: dmx += (eta/3) d/dx (v_y + w_z); then the work term dmx u0
+                    using B = Bx<BX_I>;
+                    float col[16];
+#pragma unroll
+                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        dmx[i] = cd1acc(dmx[i], col, i + 4, cf.mx[0]);
+                        de[i] = fmaf(dmx[i], c0[i], de[i]);
+                    }
+                    break;
+                }
+                case 4:
+                    lap_full(s, tj, tk, cf.vc[1], cf.vl[1][0], cf.vl[1][1], cf.vl[1][2], dmy, c0, false);
+                    break;
+                case 5: {  // SY
+                    using B = Bx<BX_J>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
+                        de[i] = fmaf(dmy[i], c0[i], de[i]);
+                    }
+                    break;
+                }
+                case 6:
+                    lap_full(s, tj, tk, cf.vc[2], cf.vl[2][0], cf.vl[2][1], cf.vl[2][2], dmz, c0, false);
+                    break;
+                case 7: {  // SZ
+                    using B = Bx<BX_K>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.mx[2]);
+                        de[i] = fmaf(dmz[i], c0[i], de[i]);
+                    }
+                    break;
+                }
+                case 8: {  // PMX: f0 = -d(rho u)/dx
+                    using B = Bx<BX_I>;
+                    float col[16];
+#pragma unroll
+                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+                    for (int i = 0; i < XI; i++) f0[i] = cd1(col, i + 4, cf.ha[0]);
+                    break;
+                }
+                case 9: {  // PMY
+                    using B = Bx<BX_J>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+                    break;
+                }
+                case 10: {  // PMZ
+                    using B = Bx<BX_K>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                    break;
+                }
+                case 11: {  // PFUU along x -> f1 (in dmx)
+                    using B = Bx<BX_I>;
+                    float col[16];
+#pragma unroll
+                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+                    for (int i = 0; i < XI; i++) dmx[i] = cd1acc(dmx[i], col, i + 4, cf.ha[0]);
+                    break;
+                }
+                case 12: {  // PFUV: along y -> f1, along x -> f2 (in dmy)
+                    using B = Bx<BX_IJ>;
+                    float col[16];
+#pragma unroll
+                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk)];
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj + 4, tk), B::K, cf.ha[1]);
+                        dmy[i] = cd1acc(dmy[i], col, i + 4, cf.ha[0]);
+                    }
+                    break;
+                }
+                case 13: {  // PFUW: along z -> f1, along x -> f3 (in dmz)
+                    using B = Bx<BX_IK>;
+                    float col[16];
+#pragma unroll
+                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk + 4)];
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj, tk + 4), 1, cf.ha[2]);
+                        dmz[i] = cd1acc(dmz[i], col, i + 4, cf.ha[0]);
+                    }
+                    break;
+                }
+                case 14: {  // PFVV along y -> f2
+                    using B = Bx<BX_J>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+                    break;
+                }
+                case 15: {  // PFVW: along z -> f2, along y -> f3
+                    using B = Bx<BX_JK>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        const float* p = s + B::at(i, tj + 4, tk + 4);
+                        dmy[i] = sd1acc(dmy[i], p, 1, cf.ha[2]);
+                        dmz[i] = sd1acc(dmz[i], p, B::K, cf.ha[1]);
+                    }
+                    break;
+                }
+                case 16: {  // PFWW along z -> f3
+                    using B = Bx<BX_K>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                    break;
+                }
+                case 17: {  // PHU along x -> f4 (in de)
+                    using B = Bx<BX_I>;
+                    float col[16];
+#pragma unroll
+                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+                    for (int i = 0; i < XI; i++) de[i] = cd1acc(de[i], col, i + 4, cf.ha[0]);
+                    break;
+                }
+                case 18: {  // PHV
+                    using B = Bx<BX_J>;
+#pragma unroll
+                    for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+                    break;
+                }
+                default: {  // 19, PHW; then -H_ref div(u) (the P set holds ((E+p) - H_ref) u), with
+                           // div(u) = (S_x + S_y + S_z) / 2 read at the cell (S is L2-resident)
+                    using B = Bx<BX_K>;
+                    const float href = -(float)b.sc->H_ref;
+                    const float* S = (const float*)b.S;
+                    const int j = min(T.j0 + tj, b.n[1] - 1), k = min(T.k0 + tk, b.n[2] - 1);
+#pragma unroll
+                    for (int i = 0; i < XI; i++) {
+                        const long long c = cell_off(b, min(T.i0 + i, b.n[0] - 1), j, k);
+                        const float hsum = __ldg(S + SX * b.fs + c) + __ldg(S + SY * b.fs + c) + __ldg(S + SZ * b.fs + c);
+                        const float a = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                        de[i] = fmaf(href, 0.5f * hsum, a);
+                    }
+                    break;
+                }
+            }
+            __syncthreads();  // buffer g & 1 is free for load g + 2
+        }
+        // RK3 stage combine (FP64) and the fused write-back, as in k_assemble
+        const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
+        float* Pw = (float*)b.P[pr ^ 1];
+        const double dt = b.sc->dt;
+        const int j = T.j0 + tj, k = T.k0 + tk;
+        double cmax = 0.0;
+        int health = 0;
+#pragma unroll
+        for (int i = 0; i < XI; i++) {
+            const int ic = T.i0 + i;
+            if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+            const long long c = cell_off(b, ic, j, k), fs = b.fs;
+            const float f[5] = {f0[i], dmx[i], dmy[i], dmz[i], de[i]};
+            double un[5];
+#pragma unroll
+            for (int l = 0; l < 5; l++) {
+                const long long e = c + l * fs;
+                const double r = (double)f[l];
+                if (STAGE == 1) {
+                    un[l] = fma(dt, r, b.U[e]);
+                    b.Us[e] = un[l];
+                } else if (STAGE == 2) {
+                    un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                    b.Us[e] = un[l];
+                } else {
+                    un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
+                    b.U[e] = un[l];
+                }
+            }
+            const double cour = epilogue<float>(b, Pw, c, ic, j, k, un, STAGE == 3, &health);
+            cmax = cour > cmax ? cour : cmax;
+        }
+        if (health) atomicOr(&b.sc->status, health);
+        if (STAGE == 3) courant_fold(b, cmax);
+    }
+}
+
+// ---- host side -------------------------------------------------------------------------------
+constexpr size_t kTmaSmem = 2 * kBufElems * sizeof(float) + 2 * sizeof(uint64_t);
+
+void tma_tile_shape(int* ti, int* tj, int* tk) {
+    *ti = XI;
+    *tj = XJ;
+    *tk = XK;
+}
+size_t tma_maps_bytes() { return sizeof(TmaMaps); }
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encoder() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// Encode the tensor maps of a mixed box into host memory `out` (sizeof(TmaMaps) bytes).
+cudaError_t tma_encode_maps(const BoxView& v, void* out) {
+    EncodeTiledFn enc = encoder();
+    if (!enc) return cudaErrorNotSupported;
+    TmaMaps* m = (TmaMaps*)out;
+    const cuuint64_t g0 = v.n[0] + 2 * CNS_NG, g1 = v.n[1] + 2 * CNS_NG, g2 = v.n[2] + 2 * CNS_NG;
+    auto one = [&](CUtensorMap* map, void* base, int nfields, int shape) -> bool {
+        const cuuint64_t dims[4] = {g2, g1, g0, (cuuint64_t)nfields};
+        const cuuint64_t strides[3] = {(cuuint64_t)v.sj * 4, (cuuint64_t)v.si * 4, (cuuint64_t)v.fs * 4};
+        const cuuint32_t box[4] = {(cuuint32_t)box_k(shape), (cuuint32_t)box_j(shape), (cuuint32_t)box_i(shape), 1};
+        const cuuint32_t es[4] = {1, 1, 1, 1};
+        return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    for (int set = 0; set < 2; set++)
+        for (int sh = 0; sh < 7; sh++)
+            if (!one(&m->p[set][sh], v.P[set], NPF, sh)) return cudaErrorInvalidValue;
+    const int sshape[4] = {BX_I, BX_J, BX_K, BX_C};
+    for (int q = 0; q < 4; q++)
+        if (!one(&m->s[q], v.S, NSF, sshape[q])) return cudaErrorInvalidValue;
+    return cudaSuccess;
+}
+
+template <int STAGE>
+static cudaError_t launch_tma_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
+    auto fn = k_assemble_tma<STAGE>;
+    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kTileThreads, kTmaSmem);
+    if (per < 1) per = 1;
+    const int grid = ntiles < nsm * per ? ntiles : nsm * per;
+    fn<<<grid, kTileThreads, kTmaSmem, st>>>(boxes, tiles, ntiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (stage == 1) return launch_tma_stage<1>(boxes, tiles, ntiles, st);
+    if (stage == 2) return launch_tma_stage<2>(boxes, tiles, ntiles, st);
+    return launch_tma_stage<3>(boxes, tiles, ntiles, st);
+}
+
+}  // namespace cns

@@ -53,6 +53,7 @@ class Done:
     admitted: float
     finished: float
     result: Optional[np.ndarray] = None
+    health: int = 0           # non-zero: the solve's state went non-physical (HEALTH_* bits)
 
     @property
     def latency(self) -> float:
@@ -148,12 +149,13 @@ class Server:
                     k += 1
                     if k >= req.steps:
                         batch.remove(box)
-                        box.sync()  # raises CnsError if this box's state went bad
-                        res = box.download() if self.keep_results else None
+                        # a solve whose state went non-physical fails alone; the others go on
+                        health = box.health()
+                        res = box.download() if (self.keep_results and not health) else None
                         box.close()
                         used -= need
                         del active[rid]
-                        done.append(Done(req, adm, fin, res))
+                        done.append(Done(req, adm, fin, res, health))
                     else:
                         active[rid] = (box, req, k, need, adm)
         finally:
@@ -166,6 +168,7 @@ class Server:
         first = min((r.arrival for r in requests), default=0.0)
         return {
             "requests": len(done),
+            "failed": sum(1 for d in done if d.health),
             "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)),
             "latency_max_s": float(lat.max()),

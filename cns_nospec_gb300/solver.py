@@ -198,11 +198,21 @@ class Box:
         L.check(self.lib.cns_box_set_tile(self.h, (C.c_int * 3)(*tlog)))
 
     def autotune(self, trial_steps=2):
-        """Pick the fastest tile shape by timing trial steps (state restored afterwards)."""
+        """Pick the fastest tile shape (and, for mixed boxes, assembly kernel) by timing trial
+        steps (state restored afterwards).  Returns (tile log2 shape, kernel, ms per step)."""
         t = (C.c_int * 3)()
+        k = C.c_int()
         ms = C.c_double()
-        L.check(self.lib.cns_box_autotune(self.h, int(trial_steps), t, C.byref(ms)))
-        return tuple(t), ms.value
+        L.check(self.lib.cns_box_autotune(self.h, int(trial_steps), t, C.byref(k), C.byref(ms)))
+        return tuple(t), k.value, ms.value
+
+    def kernel(self) -> int:
+        k = C.c_int()
+        L.check(self.lib.cns_box_get_kernel(self.h, C.byref(k)))
+        return k.value
+
+    def set_kernel(self, kernel: int):
+        L.check(self.lib.cns_box_set_kernel(self.h, int(kernel)))
 
     def launches_per_step(self) -> int:
         return int(self.lib.cns_box_launches_per_step(self.h))

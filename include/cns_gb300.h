@@ -199,11 +199,20 @@ int cns_batch_sync(cns_batch *batch);
  * A new box starts on the candidate shape that pads it least. */
 int cns_box_get_tile(const cns_box *box, int tlog[3]);
 int cns_box_set_tile(cns_box *box, const int tlog[3]);
-/* Time trial_steps RK3 steps of the box on every candidate shape and keep the fastest; the
- * box's state is restored afterwards, so the run continues bit for bit.  Blocks. */
-int cns_box_autotune(cns_box *box, int trial_steps, int tlog_out[3], double *best_ms_per_step);
-/* Same for a batch: policy 0 = every member on its least-padding shape, 1 + s = every member
- * on candidate shape s; the fastest policy is kept and the graph re-captured. */
+/* Assembly kernel of a box: CNS_ASSEMBLE_DIRECT (one cell per thread, stencil taps loaded
+ * through L1) or CNS_ASSEMBLE_TMA (mixed boxes only: 8x8x32-cell tiles whose 20 stencil fields
+ * are staged in shared memory by TMA tensor copies).  Both give identical bits.  A new mixed box
+ * starts on TMA when the driver provides the tensor-map encoder. */
+enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1 };
+int cns_box_get_kernel(const cns_box *box, int *kernel);
+int cns_box_set_kernel(cns_box *box, int kernel);
+/* Time trial_steps RK3 steps of the box on every candidate shape (and, for mixed boxes, both
+ * assembly kernels) and keep the fastest; the box's state is restored afterwards, so the run
+ * continues bit for bit.  Blocks. */
+int cns_box_autotune(cns_box *box, int trial_steps, int tlog_out[3], int *kernel_out, double *best_ms_per_step);
+/* Same for a batch.  Policy p = shape + 13 * kernel: shape 0 = every member on its
+ * least-padding shape, 1 + s = every member on candidate shape s; kernel = the assembly kernel
+ * of its mixed members.  The fastest policy is kept and the graph re-captured. */
 int cns_batch_autotune(cns_batch *batch, int trial_steps, int *chosen_policy, double *best_ms_per_step);
 
 #ifdef __cplusplus

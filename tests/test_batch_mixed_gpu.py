@@ -145,10 +145,34 @@ def test_autotune_keeps_results_and_state(gpu, cns):
     batch.close()
     box = cns.Box(24, I.box_dx(24), I.CFL, I.ETA, I.ALAM)
     box.upload(I.initial_state(24, perturb=1e-3, seed=3))
-    t, ms = box.autotune(trial_steps=1)
-    assert sum(t) == 8 and ms > 0
+    t, k, ms = box.autotune(trial_steps=1)
+    assert sum(t) == 8 and k == 0 and ms > 0
     box.advance(2)
     other = cns.Box(24, I.box_dx(24), I.CFL, I.ETA, I.ALAM)
     other.upload(I.initial_state(24, perturb=1e-3, seed=3))
     other.advance(2)
     assert np.array_equal(box.download(), other.download())
+
+
+@pytest.mark.parametrize("n", [(19, 23, 37), (8, 8, 32), (33, 17, 40), (64, 64, 64)])
+def test_tma_assembly_equals_direct_bitwise(gpu, cns, n):
+    """The TMA-staged assembly and the direct one do the same arithmetic in the same order."""
+    U0 = I.initial_state(n, perturb=1e-3, seed=17)
+    out = []
+    for kern in (cns.CNS_ASSEMBLE_DIRECT, cns.CNS_ASSEMBLE_TMA):
+        b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=cns.CNS_MIXED)
+        b.set_kernel(kern)
+        assert b.kernel() == kern
+        b.upload(U0)
+        b.advance(4)
+        b.sync()
+        out.append(b.download())
+        b.close()
+    assert np.array_equal(out[0], out[1])
+
+
+def test_tma_kernel_refused_for_fp64_boxes(gpu, cns):
+    b = cns.Box(16, I.box_dx(16), I.CFL, I.ETA, I.ALAM)
+    assert b.kernel() == cns.CNS_ASSEMBLE_DIRECT
+    with pytest.raises(cns.CnsError):
+        b.set_kernel(cns.CNS_ASSEMBLE_TMA)

@@ -24,6 +24,10 @@ class FakeBox:
     def sync(self):
         pass
 
+    def health(self):
+        # a request whose seed is negative stands for a solve that went non-physical
+        return 4 if self.seed < 0 else 0
+
     def download(self):
         return np.full(1, float(self.steps))
 
@@ -108,3 +112,42 @@ def test_served_results_equal_alone_bitwise(gpu, cns):
     assert rep["peak_bytes"] <= budget
     for d in rep["done"]:
         assert np.array_equal(d.result, S.run_alone(d.req)), d.req
+
+
+def test_a_failing_solve_fails_alone():
+    reqs = [S.Request(i, 0.0, (6, 6, 6), 4, 0, seed=(-1 if i == 2 else 1)) for i in range(5)]
+    srv = S.Server(budget_bytes=1e9, keep_results=True, box_cls=FakeBox, batch_cls=FakeBatch)
+    rep = srv.run(reqs, realtime=False)
+    assert rep["requests"] == 5 and rep["failed"] == 1
+    for d in rep["done"]:
+        if d.req.rid == 2:
+            assert d.health and d.result is None
+        else:
+            assert d.health == 0 and d.result[0] == 4
+
+
+@pytest.mark.gpu
+def test_diverging_box_does_not_disturb_its_batch(gpu, cns):
+    """A box whose state goes non-physical (negative density planted at upload) is flagged;
+    the boxes sharing its launches still equal their solo runs bit for bit."""
+    from cns_nospec_gb300 import initdata as I
+    good = [S.Request(i, 0.0, (20, 16, 24), 6, i % 2, seed=40 + i) for i in range(3)]
+    batch = cns.Batch()
+    boxes = []
+    for r in good:
+        b = cns.Box(r.n, I.box_dx(r.n), I.CFL, r.eta, r.alam, precision=r.precision)
+        b.init_field(r.amp, r.perturb, r.seed)
+        batch.add(b)
+        boxes.append(b)
+    U = I.initial_state((16, 16, 16))
+    U[10, 10, 10, 0] = -1e-3
+    bad = cns.Box(16, I.box_dx(16), I.CFL, I.ETA, I.ALAM)
+    bad.upload(U)
+    batch.add(bad)
+    batch.advance(6)
+    batch.sync()
+    assert bad.health() != 0
+    for r, b in zip(good, boxes):
+        assert b.health() == 0
+        assert np.array_equal(b.download(), S.run_alone(r))
+    batch.close()
