@@ -45,14 +45,14 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--n", type=int, default=128, help="cells per axis of the periodic box")
+    p.add_argument("--size", dest="n", type=int, default=128, help="cells per axis of the periodic box")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     p.add_argument("--case", choices=["fp64", "mixed"], default=None,
                    help="profiling case: only upload + warmup + steps of one form (for ncu), then exit")
     p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve"], default="box",
                    help="box: the headline 128^3 line (default); batch: 256 uneven boxes; "
-                        "mixed256: FP64 vs mixed at --n (use 256); serve: the request stream")
+                        "mixed256: FP64 vs mixed at --size (use 256); serve: the request stream")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     p.add_argument("--boxes", type=int, default=256)
     p.add_argument("--rate", type=float, default=3.0, help="serve: requests per second")
