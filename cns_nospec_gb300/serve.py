@@ -54,6 +54,7 @@ class Done:
     finished: float
     result: Optional[np.ndarray] = None
     health: int = 0           # non-zero: the solve's state went non-physical (HEALTH_* bits)
+    steps_done: int = 0       # RK3 steps the device ran for it (fewer than asked if evicted)
 
     @property
     def latency(self) -> float:
@@ -97,6 +98,7 @@ class Server:
     budget_bytes: float = 120e9
     max_active: int = 1 << 30
     keep_results: bool = False
+    health_every: int = 16     # check the active boxes' health every this many steps (0 = only at the end)
     box_cls: type = Box        # the device backend (tests substitute a host fake)
     batch_cls: type = Batch
     log: List[dict] = field(default_factory=list)
@@ -112,6 +114,7 @@ class Server:
         used = 0
         peak_used = 0
         iters = 0
+        executed = 0
         busy = 0.0
         t0 = time.perf_counter()
         try:
@@ -143,11 +146,14 @@ class Server:
                 batch.sync()
                 busy += time.perf_counter() - ts
                 iters += 1
+                executed += sum(r.n[0] * r.n[1] * r.n[2] for _, r, *_ in active.values())
                 fin = time.perf_counter() - t0
+                check = self.health_every > 0 and iters % self.health_every == 0
                 for rid in list(active):
                     box, req, k, need, adm = active[rid]
                     k += 1
-                    if k >= req.steps:
+                    # evict a diverged solve early instead of running it to its last step
+                    if k >= req.steps or (check and box.health()):
                         batch.remove(box)
                         # a solve whose state went non-physical fails alone; the others go on
                         health = box.health()
@@ -155,7 +161,7 @@ class Server:
                         box.close()
                         used -= need
                         del active[rid]
-                        done.append(Done(req, adm, fin, res, health))
+                        done.append(Done(req, adm, fin, res, health, k))
                     else:
                         active[rid] = (box, req, k, need, adm)
         finally:
@@ -163,18 +169,21 @@ class Server:
                 box.close()
             batch.close()
         wall = time.perf_counter() - t0
-        lat = np.array([d.latency for d in done]) if done else np.zeros(1)
-        work = sum(d.req.work for d in done)
+        ok = [d for d in done if not d.health]
+        lat = np.array([d.latency for d in ok]) if ok else np.zeros(1)
+        work = sum(d.req.work for d in ok)
         first = min((r.arrival for r in requests), default=0.0)
         return {
             "requests": len(done),
-            "failed": sum(1 for d in done if d.health),
+            "failed": len(done) - len(ok),
             "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)),
             "latency_max_s": float(lat.max()),
-            "cell_updates": work,
+            "cell_updates": work,                 # of the solves that finished healthy
+            "cell_updates_executed": executed,    # everything the device advanced, failed solves included
             "cell_updates_per_s": work / max(wall - (first if realtime else 0.0), 1e-9),
             "cell_updates_per_busy_s": work / max(busy, 1e-9),
+            "executed_per_busy_s": executed / max(busy, 1e-9),
             "busy_s": busy,
             "wall_s": wall,
             "iterations": iters,
