@@ -52,7 +52,6 @@ SIGNATURES = {
     "cns_set_device": (C.c_int, [C.c_int]),
     "cns_device_synchronize": (C.c_int, []),
     "cns_measure_fp64_peak": (C.c_int, [_D]),
-    "cns_selftest_conversions": (C.c_int, [C.c_ulonglong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]),
     "cns_ctoprim": (C.c_int, [_I, _I, _D, _D, _D, C.c_int, _D]),
     "cns_hypterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, _D]),
     "cns_diffterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, C.c_double, C.c_double]),

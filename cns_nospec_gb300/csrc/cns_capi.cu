@@ -58,11 +58,6 @@ extern "C" int cns_measure_fp64_peak(double* tflops) {
     CK(probe_fp64(tflops));
     return CNS_OK;
 }
-extern "C" int cns_selftest_conversions(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
-    if (!mismatches) return fail(CNS_ERR_INVALID, "null argument");
-    CK(selftest_conversions(n, seed, mismatches));
-    return CNS_OK;
-}
 
 // Keep freed box memory in the device's default pool instead of returning it to the driver
 // at each synchronisation, so that admitting a box after another finished costs no driver

@@ -126,32 +126,6 @@ __host__ __device__ inline long long cell_off(const BoxView& b, int i, int j, in
 // Positive doubles order like their bit patterns; the Courant max uses integer atomics.
 __device__ inline unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 
-// FP32 <-> FP64 conversions on the integer pipes.  On GB300 a hardware conversion involving
-// FP64 occupies the FP64 pipe (1/67 of the FP32 rate) like a DFMA; the mixed form converts ~14
-// values per cell and stage.  These re-bias the IEEE-754 fields instead (widening is exact;
-// narrowing rounds to nearest, ties to even, carrying into the exponent as IEEE requires) and
-// fall back to the hardware conversion for zero, subnormal, infinite, NaN or out-of-range
-// values, so every result is bit-identical to the cast.
-__device__ __forceinline__ double f2d(float x) {
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)x;
-    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
-    return __hiloint2double((int)hi, (int)(b << 29));
-}
-__device__ __forceinline__ float d2f(double x) {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const int ef = (int)((hi >> 20) & 0x7FFu) - 896;  // the float exponent field
-    if (ef <= 0 || ef >= 255) return (float)x;
-    const unsigned rest = lo & 0x1FFFFFFFu;            // the 29 bits that do not fit
-    unsigned t = ((unsigned)ef << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    t += (rest > 0x10000000u || (rest == 0x10000000u && (t & 1u))) ? 1u : 0u;
-    return __uint_as_float((hi & 0x80000000u) | t);
-}
-
-__device__ __forceinline__ double to_d(double x) { return x; }
-__device__ __forceinline__ double to_d(float x) { return f2d(x); }
-
 // Reciprocal for FP64: an FP32 seed refined by one third-order Newton-series step
 // r <- r (1 + e + e^2), e = 1 - x r (Householder's method of order 3 for 1/x).  The seed's
 // relative error e0 ~ 1e-7 becomes ~e0^3, so the result is within a few ulp of 1/x for

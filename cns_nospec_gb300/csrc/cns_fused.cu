@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
 #pragma unroll
             for (int l = 0; l < 5; l++) {
                 const long long e = c + l * fs;
-                const double r = to_d(f[l]);
+                const double r = (double)f[l];
                 if (STAGE == 1) {
                     un[l] = fma(dt, r, b.U[e]);
                     b.Us[e] = un[l];

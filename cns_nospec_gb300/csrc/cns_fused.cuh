@@ -146,22 +146,22 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
                                                   int j, int k, const double un[5], bool want_cour, int* health) {
     const long long fs = b.fs;
     const double rho = un[0], E = un[4];
-    const float rhof = d2f(rho);
+    const float rhof = (float)rho;
     const float rf = 1.0f / rhof;
-    const float mx = d2f(un[1]), my = d2f(un[2]), mz = d2f(un[3]);
+    const float mx = (float)un[1], my = (float)un[2], mz = (float)un[3];
     const float u = mx * rf, v = my * rf, w = mz * rf;
     // E/rho to ~1e-15 in FP64 from the FP32 reciprocal: y0 = E r, y = y0 + (E - rho y0) r
-    const double r64 = f2d(rf);
+    const double r64 = (double)rf;
     const double y0 = E * r64;
     const double erho = fma(fma(-rho, y0, E), r64, y0);
     const float ke = fmaf(u, u, fmaf(v, v, w * w));
-    const double eint = fma(-0.5, f2d(ke), erho);  // the cancelling subtraction, in FP64
+    const double eint = fma(-0.5, (double)ke, erho);  // the cancelling subtraction, in FP64
     // offsets from the box's reference values, formed in FP64 before rounding to FP32
     const BoxScalars& sc = *b.sc;
-    const double pd = fma(kGm1 * rho, eint, -sc.p_ref);      // p - p_ref
-    const float dp = d2f(pd);
-    const float dT = d2f((eint - sc.e_ref) * (1.0 / kCv));   // T - T_ref
-    const float dH = d2f(E - sc.E_ref) + dp;                 // (E + p) - H_ref
+    const double pd = fma(kGm1 * rho, eint, -sc.p_ref);       // p - p_ref
+    const float dp = (float)pd;
+    const float dT = (float)((eint - sc.e_ref) * (1.0 / kCv)); // T - T_ref
+    const float dH = (float)(E - sc.E_ref) + dp;               // (E + p) - H_ref
     *health |= health_bits(rho, eint);
     store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
     store_img(Pw + PV * fs, b, c, i, j, k, v, 7);

@@ -35,7 +35,6 @@ cudaError_t op_fill_ghosts_aos(double* aos, const int n[3], int nc, cudaStream_t
 cudaError_t op_aos_to_box(const double* aos, const BoxView& b, cudaStream_t st);
 cudaError_t op_box_to_aos(const BoxView& b, double* aos, int ghosts, cudaStream_t st);
 cudaError_t probe_fp64(double* tflops);
-cudaError_t selftest_conversions(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
 cudaError_t op_init_field(const BoxView& b, double ax, double ay, double az, double perturb, unsigned long long seed,
                           cudaStream_t st);
 

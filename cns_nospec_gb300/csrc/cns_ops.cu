@@ -389,48 +389,3 @@ cudaError_t op_init_field(const BoxView& b, double ax, double ay, double az, dou
     return cudaGetLastError();
 }
 }  // namespace cns
-
-// ---- self-test of the integer-pipe conversions against the hardware casts ----------------
-// Each thread draws SplitMix64 bit patterns: all 2^32 float patterns are reachable for the
-// widening check; for the narrowing check the double exponents cluster around the float
-// range, every fourth value is an exact rounding tie, and some are zero, subnormal, infinite
-// or NaN.  A mismatch is any difference in the result bits.
-namespace cns {
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
-__global__ void k_selftest_conv(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
-    unsigned long long mism = 0;
-    for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < n;
-         p += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long r = mix64(seed * 0x9E3779B97F4A7C15ull + p);
-        const float f = __uint_as_float((unsigned)r);
-        if (__double_as_longlong(f2d(f)) != __double_as_longlong((double)f)) mism++;
-        unsigned long long d = mix64(r + 1);
-        const unsigned long long e = 896 - 40 + ((d >> 52) % 340);  // exponents ~[-167, 173] unbiased
-        d = (d & 0x800FFFFFFFFFFFFFull) | (e << 52);
-        if ((p & 3) == 0) d = (d & ~0x1FFFFFFFull) | 0x10000000ull;  // exact tie
-        if ((p & 255) == 1) d &= 0x8000000000000000ull;               // signed zero
-        if ((p & 255) == 2) d = (d & 0x800FFFFFFFFFFFFFull) | (0x7FFull << 52);  // inf / NaN
-        const double x = __longlong_as_double((long long)d);
-        const float a = d2f(x), b = (float)x;
-        if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) mism++;
-    }
-    if (mism) atomicAdd(bad, mism);
-}
-
-cudaError_t selftest_conversions(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
-    unsigned long long* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, sizeof *d);
-    if (e != cudaSuccess) return e;
-    cudaMemset(d, 0, sizeof *d);
-    k_selftest_conv<<<1024, 256>>>(n, seed, d);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost);
-    cudaFree(d);
-    return e;
-}
-}  // namespace cns

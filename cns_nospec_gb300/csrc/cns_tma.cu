@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
 #pragma unroll
             for (int l = 0; l < 5; l++) {
                 const long long e = c + l * fs;
-                const double r = f2d(f[l]);
+                const double r = (double)f[l];
                 if (STAGE == 1) {
                     un[l] = fma(dt, r, b.U[e]);
                     b.Us[e] = un[l];

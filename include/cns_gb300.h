@@ -67,10 +67,6 @@ int cns_device_synchronize(void);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (a ~0.1 s probe kernel):
  * the roofline denominator of the FP64-bound stencil kernels. */
 int cns_measure_fp64_peak(double *tflops);
-/* Self-test of the library's FP32<->FP64 conversions (integer-pipe re-biasing used by the
- * mixed form) against the hardware casts on n seeded bit patterns per direction;
- * *mismatches = number of results whose bits differ (0 expected). */
-int cns_selftest_conversions(unsigned long long n, unsigned long long seed, unsigned long long *mismatches);
 
 /* ---- operator level: the reference's per-operator surface, host arrays ---------------- */
 
