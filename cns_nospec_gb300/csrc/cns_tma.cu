@@ -381,19 +381,33 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
             }
             __syncthreads();  // buffer g & 1 is free for load g + 2
         }
-        // RK3 stage combine (FP64) and the fused write-back, as in k_assemble
+        // RK3 stage combine (FP64) and the fused write-back, as in k_assemble.  The five sums
+        // of this thread's 8 cells are parked in the buffer the last field used (free: every
+        // thread passed the barrier after consuming it; each thread reads back only its own
+        // entries), so the write-back runs as a rolled loop and its code exists once, not 8x.
+        float* stash = buf[(g - 1) & 1];
+#pragma unroll
+        for (int i = 0; i < XI; i++) {
+            stash[(i * 5 + 0) * kTileThreads + tid] = f0[i];
+            stash[(i * 5 + 1) * kTileThreads + tid] = dmx[i];
+            stash[(i * 5 + 2) * kTileThreads + tid] = dmy[i];
+            stash[(i * 5 + 3) * kTileThreads + tid] = dmz[i];
+            stash[(i * 5 + 4) * kTileThreads + tid] = de[i];
+        }
         const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
         float* Pw = (float*)b.P[pr ^ 1];
         const double dt = b.sc->dt;
         const int j = T.j0 + tj, k = T.k0 + tk;
         double cmax = 0.0;
         int health = 0;
-#pragma unroll
+#pragma unroll 1
         for (int i = 0; i < XI; i++) {
             const int ic = T.i0 + i;
             if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
             const long long c = cell_off(b, ic, j, k), fs = b.fs;
-            const float f[5] = {f0[i], dmx[i], dmy[i], dmz[i], de[i]};
+            float f[5];
+#pragma unroll
+            for (int l = 0; l < 5; l++) f[l] = stash[(i * 5 + l) * kTileThreads + tid];
             double un[5];
 #pragma unroll
             for (int l = 0; l < 5; l++) {
@@ -415,6 +429,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
         }
         if (health) atomicOr(&b.sc->status, health);
         if (STAGE == 3) courant_fold(b, cmax);
+        __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
     }
 }
 
