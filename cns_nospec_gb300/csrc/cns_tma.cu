@@ -115,6 +115,23 @@ struct Bx {
 };
 
 // acc + sum_m a_m (p[+m s] - p[-m s]) on shared memory, offsets s in elements
+// Ask the copy engine to bring the FP64 state rows this tile's write-back will read into L2
+// (a hint; no data moves to the SM).  One row = the tile's k extent of one (field, i, j) line:
+// 32 doubles from element (k0 + 4), which is 16-byte aligned (rows are padded to 8 elements),
+// rounded up to an even count (16-byte size), which stays inside the padded row.
+__device__ __forceinline__ void prefetch_state_l2(const BoxView& b, const Tile& T, int stage, int tid) {
+    const int ni = min(XI, b.n[0] - T.i0), nj = min(XJ, b.n[1] - T.j0), nk = min(XK, b.n[2] - T.k0);
+    const uint32_t bytes = (uint32_t)((nk + 1) & ~1) * 8u;
+    const int rows = CNS_NC * XI * XJ;
+    for (int r = tid; r < (stage == 1 ? rows : 2 * rows); r += kTileThreads) {
+        const int rr = r % rows, l = rr / (XI * XJ), i = (rr / XJ) % XI, j = rr % XJ;
+        if (i >= ni || j >= nj) continue;
+        const double* base = r < rows ? b.U : b.Us;
+        const double* p = base + l * b.fs + cell_off(b, T.i0 + i, T.j0 + j, T.k0);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+    }
+}
+
 __device__ __forceinline__ float sd1acc(float acc, const float* p, int s, const float* a) {
     acc = fmaf(a[0], p[s] - p[-s], acc);
     acc = fmaf(a[1], p[2 * s] - p[-2 * s], acc);
@@ -205,6 +222,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
         const Tile T = tiles[tile];
         const BoxView& b = boxes[T.box];
         const CoefT<float>& cf = b.c32;
+        prefetch_state_l2(b, T, STAGE, tid);
+        // Every sum is first written, not accumulated, by its first load; clearing them here
+        // only tells the compiler that the last tile's values are dead once they are parked.
+#pragma unroll
+        for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.f;
         for (int e = 0; e < kLoads; e++, g++) {
             if (tid == 0 && g + 1 < total) {
                 const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
@@ -398,13 +420,40 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
         float* Pw = (float*)b.P[pr ^ 1];
         const double dt = b.sc->dt;
         const int j = T.j0 + tj, k = T.k0 + tk;
+        const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
+        const long long fs = b.fs;
         double cmax = 0.0;
         int health = 0;
+        // Software-pipelined: the state of cell i + 1 is loaded while cell i is computed (the
+        // loads of cells outside the box are clamped to a cell inside it and never used).
+        double nu[5], ns[5];
+        {
+            const long long c = cell_off(b, min(T.i0, b.n[0] - 1), jc, kc);
+#pragma unroll
+            for (int l = 0; l < 5; l++) {
+                nu[l] = b.U[c + l * fs];
+                ns[l] = STAGE == 1 ? 0.0 : b.Us[c + l * fs];
+            }
+        }
 #pragma unroll 1
         for (int i = 0; i < XI; i++) {
+            double u0[5], us[5];
+#pragma unroll
+            for (int l = 0; l < 5; l++) {
+                u0[l] = nu[l];
+                us[l] = ns[l];
+            }
+            if (i + 1 < XI) {
+                const long long c1 = cell_off(b, min(T.i0 + i + 1, b.n[0] - 1), jc, kc);
+#pragma unroll
+                for (int l = 0; l < 5; l++) {
+                    nu[l] = b.U[c1 + l * fs];
+                    ns[l] = STAGE == 1 ? 0.0 : b.Us[c1 + l * fs];
+                }
+            }
             const int ic = T.i0 + i;
             if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
-            const long long c = cell_off(b, ic, j, k), fs = b.fs;
+            const long long c = cell_off(b, ic, j, k);
             float f[5];
 #pragma unroll
             for (int l = 0; l < 5; l++) f[l] = stash[(i * 5 + l) * kTileThreads + tid];
@@ -414,13 +463,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
                 const long long e = c + l * fs;
                 const double r = (double)f[l];
                 if (STAGE == 1) {
-                    un[l] = fma(dt, r, b.U[e]);
+                    un[l] = fma(dt, r, u0[l]);
                     b.Us[e] = un[l];
                 } else if (STAGE == 2) {
-                    un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                    un[l] = fma(0.75, u0[l], 0.25 * fma(dt, r, us[l]));
                     b.Us[e] = un[l];
                 } else {
-                    un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
+                    un[l] = fma(1.0 / 3.0, u0[l], (2.0 / 3.0) * fma(dt, r, us[l]));
                     b.U[e] = un[l];
                 }
             }
