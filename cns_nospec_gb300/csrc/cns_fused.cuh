@@ -141,9 +141,27 @@ __device__ __forceinline__ double epilogue<double>(const BoxView& b, double* __r
     return fmax(fmax(cx, cy), cz);
 }
 
+// The mixed form's reference values (fixed per box).  A loop over cells loads them once: read
+// through the box's scalar block after each store, the compiler would have to reload them.
+struct MixedRefs {
+    double p, e, E;
+};
+__device__ __forceinline__ MixedRefs mixed_refs(const BoxView& b) {
+    const BoxScalars& sc = *b.sc;
+    return {sc.p_ref, sc.e_ref, sc.E_ref};
+}
+
+__device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
+                                                 int k, const double un[5], bool want_cour, int* health,
+                                                 const MixedRefs& sc);
 template <>
 __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __restrict__ Pw, long long c, int i,
                                                   int j, int k, const double un[5], bool want_cour, int* health) {
+    return epilogue_mixed(b, Pw, c, i, j, k, un, want_cour, health, mixed_refs(b));
+}
+__device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
+                                                 int k, const double un[5], bool want_cour, int* health,
+                                                 const MixedRefs& sc) {
     const long long fs = b.fs;
     const double rho = un[0], E = un[4];
     const float rhof = (float)rho;
@@ -157,11 +175,10 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
     const float ke = fmaf(u, u, fmaf(v, v, w * w));
     const double eint = fma(-0.5, (double)ke, erho);  // the cancelling subtraction, in FP64
     // offsets from the box's reference values, formed in FP64 before rounding to FP32
-    const BoxScalars& sc = *b.sc;
-    const double pd = fma(kGm1 * rho, eint, -sc.p_ref);       // p - p_ref
+    const double pd = fma(kGm1 * rho, eint, -sc.p);        // p - p_ref
     const float dp = (float)pd;
-    const float dT = (float)((eint - sc.e_ref) * (1.0 / kCv)); // T - T_ref
-    const float dH = (float)(E - sc.E_ref) + dp;               // (E + p) - H_ref
+    const float dT = (float)((eint - sc.e) * (1.0 / kCv));  // T - T_ref
+    const float dH = (float)(E - sc.E) + dp;                // (E + p) - H_ref
     *health |= health_bits(rho, eint);
     store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
     store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
@@ -184,7 +201,7 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
     // time each step (a drift of ~1e-7 dt per step that dominates its error against FP64).
     // Formed in FP64 once per step: 1/rho by one Newton step from the FP32 seed (~1e-14).
     const double rinv = fma(r64, fma(-rho, r64, 1.0), r64);
-    const double cs = sqrt((kGamma * (pd + sc.p_ref)) * rinv);
+    const double cs = sqrt((kGamma * (pd + sc.p)) * rinv);
     const double cx = (cs + fabs(un[1]) * rinv) * b.c64.cour[0];
     const double cy = (cs + fabs(un[2]) * rinv) * b.c64.cour[1];
     const double cz = (cs + fabs(un[3]) * rinv) * b.c64.cour[2];

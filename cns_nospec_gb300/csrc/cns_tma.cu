@@ -419,6 +419,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
         const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
         float* Pw = (float*)b.P[pr ^ 1];
         const double dt = b.sc->dt;
+        const MixedRefs refs = mixed_refs(b);
         const int j = T.j0 + tj, k = T.k0 + tk;
         const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
         const long long fs = b.fs;
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
                 ns[l] = STAGE == 1 ? 0.0 : b.Us[c + l * fs];
             }
         }
-#pragma unroll 1
+#pragma unroll 2
         for (int i = 0; i < XI; i++) {
             double u0[5], us[5];
 #pragma unroll
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
                     b.U[e] = un[l];
                 }
             }
-            const double cour = epilogue<float>(b, Pw, c, ic, j, k, un, STAGE == 3, &health);
+            const double cour = epilogue_mixed(b, Pw, c, ic, j, k, un, STAGE == 3, &health, refs);
             cmax = cour > cmax ? cour : cmax;
         }
         if (health) atomicOr(&b.sc->status, health);
