@@ -58,6 +58,7 @@ SIGNATURES = {
     "cns_diffterm_noalloc": (C.c_int, [_I, _I, C.c_int, _D, _VP, _VP, C.c_double, C.c_double, _VP]),
     "cns_fill_boundary": (C.c_int, [_D, _I, _I]),
     "cns_new_advance": (C.c_int, [C.POINTER(GlobalConst), _D, _D, _D, _D, _D, _D]),
+    "cns_host_in_place": (C.c_int, [_VP, C.c_longlong, _I]),
     "cns_advance_host": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _D]),
     "cns_box_bytes": (C.c_longlong, [C.POINTER(BoxDesc)]),
     "cns_box_create": (C.c_int, [C.POINTER(BoxDesc), C.POINTER(_VP)]),

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libcns_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["cns_fused.cu", "cns_tma.cu", "cns_ops.cu", "cns_capi.cu", "cns_io.cpp", "cns_noalloc.cu"]
+SOURCES = ["cns_fused.cu", "cns_tma.cu", "cns_ops.cu", "cns_capi.cu", "cns_io.cpp", "cns_noalloc.cu", "cns_host.cu"]
 
 
 def nvcc() -> str:

@@ -396,11 +396,43 @@ extern "C" int cns_box_upload_device(cns_box* b, const double* U_dev) {
     return prime(b);
 }
 
+// Host array -> box, primed, queued on the box's stream.  A page-locked array (h_map, its
+// device address) is read in place, interior only; for FP64 boxes the first ctoprim + Courant
+// pass is fused into that read, and with `ghosts` the array's ghost cells are written with the
+// periodic images of its interior on the way.  Otherwise it is staged through the box's AoS
+// buffer (and `ghosts` is left to the caller).
+static int upload_host(cns_box* b, const double* U_host, double* h_map, bool ghosts) {
+    if (!h_map) {
+        CK(cudaMemcpyAsync(b->d_aos, U_host, aos_bytes(b), cudaMemcpyHostToDevice, b->stream));
+        return cns_box_upload_device(b, b->d_aos);
+    }
+    const bool fp64 = b->desc.precision == CNS_FP64;
+    CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
+    CK(host_upload(b->view, h_map, fp64, ghosts, b->stream));
+    CK(launch_refs(b->d_view, 1, b->stream));
+    if (!fp64) CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->ntiles, b->stream));
+    CK(launch_stepend(b->d_view, 1, 0, b->stream));
+    b->primed = true;
+    return CNS_OK;
+}
+
+// Box -> host array (interior, and with `ghosts` every ghost cell as its periodic image),
+// queued on the box's stream; in place for a page-locked array, else staged.
+static int download_host(cns_box* b, double* U_host, double* h_map, bool ghosts) {
+    if (!h_map) {
+        CK(op_box_to_aos(b->view, b->d_aos, ghosts ? 1 : 0, b->stream));
+        CK(cudaMemcpyAsync(U_host, b->d_aos, aos_bytes(b), cudaMemcpyDeviceToHost, b->stream));
+        return CNS_OK;
+    }
+    CK(host_download(b->view, h_map, b->stream));
+    if (ghosts) CK(host_ghosts(b->view, h_map, b->stream));
+    return CNS_OK;
+}
+
 extern "C" int cns_box_upload(cns_box* b, const double* U_host) {
     if (!b || !U_host) return fail(CNS_ERR_INVALID, "null argument");
     CK(cudaSetDevice(b->dev));
-    CK(cudaMemcpyAsync(b->d_aos, U_host, aos_bytes(b), cudaMemcpyHostToDevice, b->stream));
-    int rc = cns_box_upload_device(b, b->d_aos);
+    int rc = upload_host(b, U_host, (double*)mapped_host_range(U_host, aos_bytes(b)), false);
     if (rc) return rc;
     CK(cudaStreamSynchronize(b->stream));
     return CNS_OK;
@@ -415,9 +447,9 @@ extern "C" int cns_box_download_device(cns_box* b, double* U_dev) {
 
 extern "C" int cns_box_download(cns_box* b, double* U_host) {
     if (!b || !U_host) return fail(CNS_ERR_INVALID, "null argument");
-    int rc = cns_box_download_device(b, b->d_aos);
+    CK(cudaSetDevice(b->dev));
+    int rc = download_host(b, U_host, (double*)mapped_host_range(U_host, aos_bytes(b)), true);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(U_host, b->d_aos, aos_bytes(b), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     return CNS_OK;
 }
@@ -958,16 +990,19 @@ static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt
     cns_box* b;
     int rc = cached_box(d, &b);
     if (rc) return rc;
-    const size_t bytes = aos_bytes(b);
-    CK(cudaMemcpyAsync(b->d_aos, U, bytes, cudaMemcpyHostToDevice, b->stream));
-    if ((rc = cns_box_upload_device(b, b->d_aos))) return rc;
+    double* h_map = (double*)mapped_host_range(U, aos_bytes(b));
+    // the last step's start state supplies the ghosts: with at most one step that is the input
+    const bool ghosts_on_upload = h_map && nsteps <= 1;
+    if ((rc = upload_host(b, U, h_map, ghosts_on_upload))) return rc;
     int done = 0;
     while (done < nsteps) {
         const int chunk = std::min(nsteps - done, DTLOG_CAP);
         if (done + chunk == nsteps) {
-            // the last step's start state supplies the ghosts
             if (chunk > 1 && (rc = cns_box_advance(b, chunk - 1))) return rc;
-            CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
+            if (!h_map)
+                CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
+            else if (!ghosts_on_upload)
+                CK(host_ghosts(b->view, h_map, b->stream));
             if ((rc = cns_box_advance(b, 1))) return rc;
         } else if ((rc = cns_box_advance(b, chunk))) {
             return rc;
@@ -980,9 +1015,12 @@ static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt
         }
         done += chunk;
     }
-    if (nsteps == 0) CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
-    CK(op_box_to_aos(b->view, b->d_aos, 0, b->stream));
-    CK(cudaMemcpyAsync(U, b->d_aos, bytes, cudaMemcpyDeviceToHost, b->stream));
+    if (h_map) {
+        if ((rc = download_host(b, U, h_map, false))) return rc;
+    } else {
+        if (nsteps == 0) CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
+        if ((rc = download_host(b, U, nullptr, false))) return rc;
+    }
     int health = 0;
     rc = cns_box_sync(b, &health);
     return rc;
@@ -1005,6 +1043,12 @@ extern "C" int cns_advance_host(double* U, const int n[3], const double dx[3], d
     int rc = validate_desc(&d);
     if (rc) return rc;
     return host_advance(d, U, nsteps, dt_hist);
+}
+
+extern "C" int cns_host_in_place(const void* U, long long bytes, int* in_place) {
+    if (!U || !in_place || bytes < 0) return fail(CNS_ERR_INVALID, "null argument or negative size");
+    *in_place = mapped_host_range(U, (size_t)bytes) ? 1 : 0;
+    return CNS_OK;
 }
 
 extern "C" int cns_new_advance(const cns_global_const_t* h, double* U, double* Unew, double* Q, double* D, double* F,

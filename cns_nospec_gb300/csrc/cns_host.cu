@@ -1,0 +1,229 @@
+// cns_host.cu -- the reference-layout host array <-> a box, moved by the SMs themselves over
+// the CPU-GPU link when the caller's array is page-locked (and so mapped into the device's
+// address space).
+//
+// The reference's new_advance works in place on a host array U[i][j][k][l] with 4 ghost
+// layers, component fastest (cpu/helper_functions.cpp:100-122).  Only the interior of the
+// input matters (stage 1 refills the ghosts, cpu/advance.cpp:45), and on return the ghosts hold
+// the periodic images of the last step's start state (stage 3 writes the interior only,
+// cpu/advance.cpp:144-153).  Reading and writing the caller's array in place saves the staging
+// copy in HBM and its conversion pass, moves only the interior on the way in (84 of 101 MB at
+// 128^3), and for FP64 boxes runs the first ctoprim + Courant pass in the same kernel as the
+// read, under the link time.
+//
+// One warp per run of up to 32 consecutive k cells of an (i, j) row: the run's 5 x 32 doubles
+// are contiguous in the host array and move with lane-strided (coalesced) accesses through a
+// per-warp shared-memory buffer; the device side is the box's structure-of-arrays layout.
+#include <cuda.h>
+
+#include "cns_fused.cuh"
+#include "cns_internal.h"
+
+namespace cns {
+
+constexpr int kRun = 32, kWarps = 8;
+
+struct RunIdx {
+    int i, j, k0, cnt;
+    long long a0;  // element offset of the run's first value in the host array
+};
+
+// Run w of the interior: rows (i, j) of the interior, runs of 32 along k.
+__device__ __forceinline__ RunIdx interior_run(const BoxView& b, long long w) {
+    const int runs = (b.n[2] + kRun - 1) / kRun;
+    const int g1 = b.n[1] + 2 * CNS_NG, g2 = b.n[2] + 2 * CNS_NG;
+    RunIdx r;
+    const int kr = (int)(w % runs);
+    const long long row = w / runs;
+    r.j = (int)(row % b.n[1]);
+    r.i = (int)(row / b.n[1]);
+    r.k0 = kr * kRun;
+    r.cnt = min(kRun, b.n[2] - r.k0);
+    r.a0 = (((long long)(r.i + CNS_NG) * g1 + (r.j + CNS_NG)) * g2 + (r.k0 + CNS_NG)) * CNS_NC;
+    return r;
+}
+
+// Write the run's periodic images into the host array's ghost cells: the whole run shifted by
+// +-n along i and/or j (rows of ghost cells), and its first / last 4 cells shifted along k.
+// Every ghost cell has exactly one interior source, so no cell is written twice.
+__device__ __forceinline__ void run_images(const BoxView& b, const RunIdx& r, const double* sw, double* h, int lane) {
+    const int g1 = b.n[1] + 2 * CNS_NG, g2 = b.n[2] + 2 * CNS_NG;
+    // shift number a along i: 0, then +n if the row is in the low layer, then -n if in the high
+    const bool ilo = r.i < CNS_NG, ihi = r.i >= b.n[0] - CNS_NG, jlo = r.j < CNS_NG, jhi = r.j >= b.n[1] - CNS_NG;
+    const int ni = 1 + ilo + ihi, nj = 1 + jlo + jhi;
+    const int klo = r.k0 < CNS_NG ? min(CNS_NG - r.k0, r.cnt) : 0;        // cells k < 4
+    const int khi = max(b.n[2] - CNS_NG, r.k0) - r.k0;                    // first cell k >= n-4
+    const long long kshift = (long long)b.n[2] * CNS_NC;
+    for (int a = 0; a < ni; a++) {
+        for (int c = 0; c < nj; c++) {
+            const int di = a == 0 ? 0 : (a == 1 && ilo ? b.n[0] : -b.n[0]);
+            const int dj = c == 0 ? 0 : (c == 1 && jlo ? b.n[1] : -b.n[1]);
+            const long long base = r.a0 + ((long long)di * g1 + dj) * g2 * CNS_NC;
+            if (a || c)
+                for (int q = lane; q < r.cnt * CNS_NC; q += 32) h[base + q] = sw[q];
+            for (int q = lane; q < klo * CNS_NC; q += 32) h[base + kshift + q] = sw[q];
+            for (int q = khi * CNS_NC + lane; q < r.cnt * CNS_NC; q += 32) h[base - kshift + q] = sw[q];
+        }
+    }
+}
+
+// Host interior -> box U; with PRIM also the P set (with its ghost images), the health bits and
+// the Courant number of the state, as k_prim does; with GHOSTS also the host array's ghost
+// cells as the periodic images of its interior (what the reference's fill_boundary leaves
+// there), written back over the link while the interior is read.
+template <bool PRIM, bool GHOSTS>
+__global__ void __launch_bounds__(kWarps * 32) k_host_upload(BoxView b, double* __restrict__ h) {
+    __shared__ double s[kWarps][kRun * CNS_NC];
+    const int lane = threadIdx.x & 31;
+    double* sw = s[threadIdx.x >> 5];
+    const long long nw = (long long)b.n[0] * b.n[1] * ((b.n[2] + kRun - 1) / kRun);
+    for (long long w = blockIdx.x * (long long)kWarps + (threadIdx.x >> 5); w < nw; w += (long long)gridDim.x * kWarps) {
+        const RunIdx r = interior_run(b, w);
+        for (int q = lane; q < r.cnt * CNS_NC; q += 32) sw[q] = h[r.a0 + q];
+        __syncwarp();
+        if (GHOSTS) run_images(b, r, sw, h, lane);
+        double cour = 0.0;
+        int health = 0;
+        if (lane < r.cnt) {
+            const int k = r.k0 + lane;
+            const long long c = cell_off(b, r.i, r.j, k);
+            double un[CNS_NC];
+#pragma unroll
+            for (int l = 0; l < CNS_NC; l++) {
+                un[l] = sw[lane * CNS_NC + l];
+                b.U[c + l * b.fs] = un[l];
+            }
+            if (PRIM) cour = epilogue<double>(b, (double*)b.P[b.sc->pbase], c, r.i, r.j, k, un, true, &health);
+        }
+        if (PRIM) {
+            if (health) atomicOr(&b.sc->status, health);
+            courant_fold(b, cour);  // the whole warp takes part (w is warp-uniform)
+        }
+        __syncwarp();
+    }
+}
+
+// Box U interior -> host interior.
+__global__ void __launch_bounds__(kWarps * 32) k_host_download(BoxView b, double* __restrict__ h) {
+    __shared__ double s[kWarps][kRun * CNS_NC];
+    const int lane = threadIdx.x & 31;
+    double* sw = s[threadIdx.x >> 5];
+    const long long nw = (long long)b.n[0] * b.n[1] * ((b.n[2] + kRun - 1) / kRun);
+    for (long long w = blockIdx.x * (long long)kWarps + (threadIdx.x >> 5); w < nw; w += (long long)gridDim.x * kWarps) {
+        const RunIdx r = interior_run(b, w);
+        if (lane < r.cnt) {
+            const long long c = cell_off(b, r.i, r.j, r.k0 + lane);
+#pragma unroll
+            for (int l = 0; l < CNS_NC; l++) sw[lane * CNS_NC + l] = b.U[c + l * b.fs];
+        }
+        __syncwarp();
+        for (int q = lane; q < r.cnt * CNS_NC; q += 32) h[r.a0 + q] = sw[q];
+        __syncwarp();
+    }
+}
+
+// Every ghost cell of the host array <- the periodic image of the box's current U (what the
+// reference's fill_boundary leaves there, cpu/helper_functions.cpp:226-262).  Runs of 32 along
+// k over all ghost-inclusive rows; a run with no ghost cell is skipped.
+__global__ void __launch_bounds__(kWarps * 32) k_host_ghosts(BoxView b, double* __restrict__ h) {
+    __shared__ double s[kWarps][kRun * CNS_NC];
+    const int lane = threadIdx.x & 31;
+    double* sw = s[threadIdx.x >> 5];
+    const int g0 = b.n[0] + 2 * CNS_NG, g1 = b.n[1] + 2 * CNS_NG, g2 = b.n[2] + 2 * CNS_NG;
+    const int runs = (g2 + kRun - 1) / kRun;
+    const long long nw = (long long)g0 * g1 * runs;
+    for (long long w = blockIdx.x * (long long)kWarps + (threadIdx.x >> 5); w < nw; w += (long long)gridDim.x * kWarps) {
+        const int kr = (int)(w % runs);
+        const long long row = w / runs;
+        const int J = (int)(row % g1), I = (int)(row / g1);
+        const bool ghost_row = I < CNS_NG || I >= b.n[0] + CNS_NG || J < CNS_NG || J >= b.n[1] + CNS_NG;
+        const int K0 = kr * kRun, cnt = min(kRun, g2 - K0);
+        if (!ghost_row && K0 >= CNS_NG && K0 + cnt <= b.n[2] + CNS_NG) continue;  // warp-uniform
+        const long long a0 = (((long long)I * g1 + J) * g2 + K0) * CNS_NC;
+        if (lane < cnt) {
+            const int K = K0 + lane;
+            const int ii = (I - CNS_NG + b.n[0]) % b.n[0], jj = (J - CNS_NG + b.n[1]) % b.n[1],
+                      kk = (K - CNS_NG + b.n[2]) % b.n[2];
+            const long long c = cell_off(b, ii, jj, kk);
+#pragma unroll
+            for (int l = 0; l < CNS_NC; l++) sw[lane * CNS_NC + l] = b.U[c + l * b.fs];
+        }
+        __syncwarp();
+        for (int q = lane; q < cnt * CNS_NC; q += 32) {
+            const int K = K0 + q / CNS_NC;
+            if (ghost_row || K < CNS_NG || K >= b.n[2] + CNS_NG) h[a0 + q] = sw[q];
+        }
+        __syncwarp();
+    }
+}
+
+static int run_blocks(long long warps) {
+    const long long b = (warps + kWarps - 1) / kWarps;
+    return (int)(b > 1048576 ? 1048576 : (b < 1 ? 1 : b));
+}
+
+cudaError_t host_upload(const BoxView& v, double* h, bool prim, bool ghosts, cudaStream_t st) {
+    const long long nw = (long long)v.n[0] * v.n[1] * ((v.n[2] + kRun - 1) / kRun);
+    const int nb = run_blocks(nw), nt = kWarps * 32;
+    if (prim && ghosts)
+        k_host_upload<true, true><<<nb, nt, 0, st>>>(v, h);
+    else if (prim)
+        k_host_upload<true, false><<<nb, nt, 0, st>>>(v, h);
+    else if (ghosts)
+        k_host_upload<false, true><<<nb, nt, 0, st>>>(v, h);
+    else
+        k_host_upload<false, false><<<nb, nt, 0, st>>>(v, h);
+    return cudaGetLastError();
+}
+
+cudaError_t host_download(const BoxView& v, double* h, cudaStream_t st) {
+    const long long nw = (long long)v.n[0] * v.n[1] * ((v.n[2] + kRun - 1) / kRun);
+    k_host_download<<<run_blocks(nw), kWarps * 32, 0, st>>>(v, h);
+    return cudaGetLastError();
+}
+
+cudaError_t host_ghosts(const BoxView& v, double* h, cudaStream_t st) {
+    const long long nw = (long long)(v.n[0] + 2 * CNS_NG) * (v.n[1] + 2 * CNS_NG) * ((v.n[2] + 2 * CNS_NG + kRun - 1) / kRun);
+    k_host_ghosts<<<run_blocks(nw), kWarps * 32, 0, st>>>(v, h);
+    return cudaGetLastError();
+}
+
+// The device address of the host range [p, p + bytes) when all of it lies inside one
+// page-locked allocation that the device can address; otherwise null (the caller then stages
+// through a copy).  The range is checked against the allocation's extent as the driver records
+// it, so a kernel never touches host memory outside the caller's allocation.
+typedef CUresult (*PointerGetAttributeFn)(void*, CUpointer_attribute, CUdeviceptr);
+
+static PointerGetAttributeFn pointer_attr_fn() {
+    static PointerGetAttributeFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PointerGetAttributeFn)p;
+    }
+    return fn;
+}
+
+void* mapped_host_range(const void* p, size_t bytes) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // not a pointer the runtime knows; clear the (non-sticky) error
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    PointerGetAttributeFn get = pointer_attr_fn();
+    if (!get) return nullptr;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    const CUdeviceptr dp = (CUdeviceptr)a.devicePointer;
+    if (get(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, dp) != CUDA_SUCCESS) return nullptr;
+    if (get(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, dp) != CUDA_SUCCESS) return nullptr;
+    if (dp < start || dp - start > size || bytes > size - (size_t)(dp - start)) return nullptr;
+    return a.devicePointer;
+}
+
+}  // namespace cns

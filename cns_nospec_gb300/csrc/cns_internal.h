@@ -35,6 +35,14 @@ cudaError_t op_fill_ghosts_aos(double* aos, const int n[3], int nc, cudaStream_t
 cudaError_t op_aos_to_box(const double* aos, const BoxView& b, cudaStream_t st);
 cudaError_t op_box_to_aos(const BoxView& b, double* aos, int ghosts, cudaStream_t st);
 cudaError_t probe_fp64(double* tflops);
+
+// the reference-layout host array <-> a box over the CPU-GPU link, in place (cns_host.cu).
+// `h` is the device address of a page-locked host array (mapped_host_range).
+void* mapped_host_range(const void* p, size_t bytes);
+// ghosts: also write the host array's ghost cells (periodic images of its interior)
+cudaError_t host_upload(const BoxView& v, double* h, bool prim, bool ghosts, cudaStream_t st);
+cudaError_t host_download(const BoxView& v, double* h, cudaStream_t st);
+cudaError_t host_ghosts(const BoxView& v, double* h, cudaStream_t st);
 cudaError_t op_init_field(const BoxView& b, double ax, double ay, double az, double perturb, unsigned long long seed,
                           cudaStream_t st);
 

@@ -118,6 +118,14 @@ int cns_new_advance(const cns_global_const_t *h, double *U, double *Unew, double
 int cns_advance_host(double *U, const int n[3], const double dx[3], double cfl, double eta, double alam,
                      int nsteps, int precision, double *dt_hist);
 
+/* Host arrays: when all of [U, U + bytes) lies in one page-locked allocation the device can
+ * address (cudaHostAlloc, cudaHostRegister, a pinned torch tensor), cns_new_advance,
+ * cns_advance_host, cns_box_upload and cns_box_download read and write it in place from the
+ * GPU over the CPU-GPU link (interior only on the way in; no staging copy); any other host
+ * memory is staged through a device buffer.  Results are bit-identical either way.
+ * *in_place = 1 when `U` takes the in-place path.  No counterpart in the reference. */
+int cns_host_in_place(const void *U, long long bytes, int *in_place);
+
 /* ---- device-resident boxes ------------------------------------------------------------- */
 typedef struct cns_box cns_box;
 

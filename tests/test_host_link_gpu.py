@@ -1,0 +1,94 @@
+"""Host arrays moved in place by the GPU over the CPU-GPU link (page-locked memory) against the
+staged path (pageable memory): bit-identical results from cns_new_advance, cns_advance_host
+(FP64 and mixed; 0, 1 and 3 steps; a non-cubic box) and Box upload/download, ghost cells
+included.  The input's ghost cells are filled with garbage: only the interior may be read."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def pinned_copy(a):
+    t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+    out = t.numpy()
+    out[...] = a
+    return out, t  # the tensor owns the page-locked memory
+
+
+def garbage_ghosts(U, seed):
+    rng = np.random.default_rng(seed)
+    G = U.copy()
+    inner = np.zeros(U.shape[:3], dtype=bool)
+    inner[4:-4, 4:-4, 4:-4] = True
+    G[~inner] = rng.uniform(-1e3, 1e3, size=(int((~inner).sum()), U.shape[3]))
+    return G
+
+
+def in_place(lib, a, nbytes=None):
+    flag = ctypes.c_int(-1)
+    nb = a.nbytes if nbytes is None else nbytes
+    assert lib.cns_host_in_place(ctypes.c_void_p(a.ctypes.data), ctypes.c_longlong(nb), ctypes.byref(flag)) == 0
+    return flag.value
+
+
+def test_in_place_query(gpu, cns):
+    a = np.zeros((8, 8, 8, 5))
+    p, _keep = pinned_copy(a)
+    assert in_place(gpu, p) == 1
+    assert in_place(gpu, a) == 0
+    # a range running past the end of the page-locked allocation is refused
+    assert in_place(gpu, p, nbytes=1 << 40) == 0
+
+
+def test_new_advance_pinned_equals_pageable(gpu, cns):
+    from cns_nospec_gb300 import initdata as I
+    n = 24
+    U0 = garbage_ghosts(I.initial_state(n, perturb=1e-3, seed=5), 1)
+    h = cns.read_configurations(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    Ua = U0.copy()
+    Ub, _keep = pinned_copy(U0)
+    assert in_place(gpu, Ub) == 1
+    for _ in range(2):
+        dta = cns.new_advance(Ua, None, None, None, None, h)
+        dtb = cns.new_advance(Ub, None, None, None, None, h)
+        assert dta == dtb
+        assert np.array_equal(Ua.view(np.uint64), Ub.view(np.uint64))
+
+
+@pytest.mark.parametrize("precision,n", [(0, (20, 12, 36)), (1, (20, 12, 36)), (0, (4, 5, 6))])
+@pytest.mark.parametrize("nsteps", [0, 1, 3])
+def test_advance_host_pinned_equals_pageable(gpu, cns, precision, n, nsteps):
+    # (4, 5, 6): every interior cell is within 4 of both faces, so each has images on both sides
+    from cns_nospec_gb300 import initdata as I
+    U0 = garbage_ghosts(I.initial_state(n, perturb=1e-3, seed=7), 2)
+    Ua = U0.copy()
+    Ub, _keep = pinned_copy(U0)
+    dta = cns.advance_host(Ua, nsteps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision)
+    dtb = cns.advance_host(Ub, nsteps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision)
+    assert np.array_equal(dta, dtb)
+    assert np.array_equal(Ua.view(np.uint64), Ub.view(np.uint64))
+    if nsteps == 0:  # the interior is unchanged and the ghosts are its periodic images
+        assert np.array_equal(Ub, I.fill_periodic(U0.copy()))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_box_upload_download_pinned_equals_pageable(gpu, cns, precision):
+    from cns_nospec_gb300 import initdata as I
+    n = (16, 28, 20)
+    U0 = garbage_ghosts(I.initial_state(n, perturb=1e-3, seed=9), 3)
+    outs = []
+    for pin in (False, True):
+        src, keep = pinned_copy(U0) if pin else (U0.copy(), None)
+        box = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=precision)
+        box.upload(src)
+        box.advance(3)
+        dst, keep2 = pinned_copy(np.full(U0.shape, np.nan)) if pin else (np.full(U0.shape, np.nan), None)
+        box.download(dst)
+        box.sync()
+        outs.append(dst.copy())
+        box.close()
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
