@@ -16,6 +16,7 @@ _VP = C.c_void_p
 
 CNS_OK, CNS_ERR_INVALID, CNS_ERR_NOMEM, CNS_ERR_NONFINITE, CNS_ERR_CUDA, CNS_ERR_CAPACITY, CNS_ERR_NODEVICE = range(7)
 CNS_FP64, CNS_MIXED = 0, 1
+CNS_HEALTH_NONPOS_RHO, CNS_HEALTH_NONFINITE, CNS_HEALTH_NONPOS_EINT, CNS_HEALTH_TIMEOUT = 1, 2, 4, 8
 CNS_ASSEMBLE_DIRECT, CNS_ASSEMBLE_TMA = 0, 1
 KERN_DERIV, KERN_ASSEMBLE, KERN_STEPEND, KERN_PRIM, KERN_COUNT = range(5)
 KERNEL_NAMES = ("k_deriv", "k_assemble", "k_stepend", "k_prim")
@@ -52,6 +53,7 @@ SIGNATURES = {
     "cns_set_device": (C.c_int, [C.c_int]),
     "cns_device_synchronize": (C.c_int, []),
     "cns_measure_fp64_peak": (C.c_int, [_D]),
+    "cns_selftest_bounded_wait": (C.c_int, [_I]),
     "cns_ctoprim": (C.c_int, [_I, _I, _D, _D, _D, C.c_int, _D]),
     "cns_hypterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, _D]),
     "cns_diffterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, C.c_double, C.c_double]),

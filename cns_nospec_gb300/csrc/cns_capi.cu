@@ -53,6 +53,12 @@ extern "C" int cns_device_synchronize(void) {
     CK(cudaDeviceSynchronize());
     return CNS_OK;
 }
+extern "C" int cns_selftest_bounded_wait(int* status) {
+    if (!status) return fail(CNS_ERR_INVALID, "null argument");
+    CK(bounded_wait_selftest(status));
+    return CNS_OK;
+}
+
 extern "C" int cns_measure_fp64_peak(double* tflops) {
     if (!tflops) return fail(CNS_ERR_INVALID, "null argument");
     CK(probe_fp64(tflops));

@@ -19,6 +19,7 @@ cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st);
 void tma_tile_shape(int* ti, int* tj, int* tk);
 size_t tma_maps_bytes();
 cudaError_t tma_encode_maps(const BoxView& v, void* out);
+cudaError_t bounded_wait_selftest(int* status);
 cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st);
 

@@ -483,6 +483,33 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
     }
 }
 
+// Self-test of the bounded wait: an mbarrier nothing ever arrives on.  The wait must give up
+// after its limit and the block must report HEALTH_TIMEOUT and return normally.
+__global__ void k_bounded_wait_selftest(int* out) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0u);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) *out = HEALTH_TIMEOUT;
+}
+
+cudaError_t bounded_wait_selftest(int* status) {
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        k_bounded_wait_selftest<<<1, 32>>>(d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e;
+}
+
 // ---- host side -------------------------------------------------------------------------------
 constexpr size_t kTmaSmem = 2 * kBufElems * sizeof(float) + 2 * sizeof(uint64_t);
 

@@ -37,6 +37,14 @@ typedef enum cns_status {
     CNS_ERR_NODEVICE = 6   /* no CUDA device */
 } cns_status;
 
+/* Health bits of a box (sticky; cns_box_sync): what made it return CNS_ERR_NONFINITE. */
+typedef enum cns_health {
+    CNS_HEALTH_NONPOS_RHO = 1,  /* density <= 0 somewhere */
+    CNS_HEALTH_NONFINITE = 2,   /* a non-finite density or internal energy */
+    CNS_HEALTH_NONPOS_EINT = 4, /* internal energy <= 0 somewhere */
+    CNS_HEALTH_TIMEOUT = 8      /* a bounded wait inside a kernel gave up; that launch returned early */
+} cns_health;
+
 typedef enum cns_precision {
     CNS_FP64 = 0, /* plain form: FP64 throughout */
     CNS_MIXED = 1 /* FP32 primitives/stencils/fluxes; FP64 e = E/rho - |u|^2/2 and RK3 state */
@@ -67,6 +75,11 @@ int cns_device_synchronize(void);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (a ~0.1 s probe kernel):
  * the roofline denominator of the FP64-bound stencil kernels. */
 int cns_measure_fp64_peak(double *tflops);
+/* Self-test of the bounded waits inside the library's kernels: one block waits on an
+ * mbarrier that nothing arrives on; the wait gives up after about one second and the block
+ * reports *status = CNS_HEALTH_TIMEOUT (8) instead of hanging.  No counterpart in the
+ * reference. */
+int cns_selftest_bounded_wait(int *status);
 
 /* ---- operator level: the reference's per-operator surface, host arrays ---------------- */
 
