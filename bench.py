@@ -325,7 +325,7 @@ def run_ours(args, dist):
                    "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
                    "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
                    "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)},
-                   "mixed_assembly_kernel": "tma" if kern32 == C.CNS_ASSEMBLE_TMA else "direct"},
+                   "mixed_assembly_kernel": {C.CNS_ASSEMBLE_TMA: "tma", C.CNS_ASSEMBLE_TMA_WS: "tma_ws"}.get(kern32, "direct")},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "api": "cns_new_advance (host U, copy in + 1 step + copy out)",
                 "pinned_host": pinned, "steps": k_e2e},

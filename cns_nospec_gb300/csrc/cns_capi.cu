@@ -305,7 +305,7 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
         maps.resize(tma_maps_bytes());
         if (tma_encode_maps(v, maps.data()) == cudaSuccess) {
             v.tma = b->arena + g.off_maps;
-            b->kernel = CNS_ASSEMBLE_TMA;
+            b->kernel = assemble_ws_fits() ? CNS_ASSEMBLE_TMA_WS : CNS_ASSEMBLE_TMA;
         }
     }
     e = cudaMemsetAsync(b->arena, 0, g.total, b->stream);
@@ -471,6 +471,8 @@ struct WorkLists {
     int na32 = 0;
     const Tile* x32 = nullptr;
     int nx32 = 0;
+    const Tile* w32 = nullptr;  // mixed boxes on the warp-specialised TMA assembly
+    int nw32 = 0;
 };
 
 // One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
@@ -508,6 +510,10 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
             CK(launch_assemble_tma(views, w.x32, w.nx32, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
+        if (w.nw32) {
+            CK(launch_assemble_ws(views, w.w32, w.nw32, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
     }
     CK(launch_stepend(views, nviews, 1, st));
     return mark(CNS_KERN_STEPEND);
@@ -519,6 +525,8 @@ static WorkLists box_lists(const cns_box* b) {
         w.d32 = b->d_tiles, w.nd32 = b->ntiles;
         if (b->kernel == CNS_ASSEMBLE_TMA)
             w.x32 = b->d_xtiles, w.nx32 = b->nxtiles;
+        else if (b->kernel == CNS_ASSEMBLE_TMA_WS)
+            w.w32 = b->d_xtiles, w.nw32 = b->nxtiles;
         else
             w.a32 = b->d_tiles, w.na32 = b->ntiles;
     } else {
@@ -726,7 +734,7 @@ extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->member
 static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
-    std::vector<Tile> d64, d32, a32, x32;  // the four lists of WorkLists
+    std::vector<Tile> d64, d32, a32, x32, w32;  // the five lists of WorkLists
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
@@ -737,12 +745,14 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
         append_tiles(b->desc.n, b->view.tlog, (int)m, d32);
         if (b->kernel == CNS_ASSEMBLE_TMA)
             append_xtiles(b->desc.n, (int)m, x32);
+        else if (b->kernel == CNS_ASSEMBLE_TMA_WS)
+            append_xtiles(b->desc.n, (int)m, w32);
         else
             append_tiles(b->desc.n, b->view.tlog, (int)m, a32);
     }
     std::vector<Tile> all;
-    all.reserve(d64.size() + d32.size() + a32.size() + x32.size());
-    for (auto* v : {&d64, &d32, &a32, &x32}) all.insert(all.end(), v->begin(), v->end());
+    all.reserve(d64.size() + d32.size() + a32.size() + x32.size() + w32.size());
+    for (auto* v : {&d64, &d32, &a32, &x32, &w32}) all.insert(all.end(), v->begin(), v->end());
     const size_t nt = all.size();
     if (views.size() > bt->cap_views) {
         cudaFree(bt->d_views);
@@ -764,7 +774,8 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     w.d64 = at, w.nd64 = (int)d64.size(), at += d64.size();
     w.d32 = at, w.nd32 = (int)d32.size(), at += d32.size();
     w.a32 = at, w.na32 = (int)a32.size(), at += a32.size();
-    w.x32 = at, w.nx32 = (int)x32.size();
+    w.x32 = at, w.nx32 = (int)x32.size(), at += x32.size();
+    w.w32 = at, w.nw32 = (int)w32.size();
     bt->nviews = (int)views.size();
     if (bt->gexec) {
         cudaGraphExecDestroy(bt->gexec);
@@ -1204,9 +1215,10 @@ static int restore_state(cns_box* b, const BoxScalars* hs) {
 }
 
 static int apply_kernel(cns_box* b, int kernel) {
-    if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA) return fail(CNS_ERR_INVALID, "unknown kernel %d", kernel);
-    if (kernel == CNS_ASSEMBLE_TMA && (b->desc.precision != CNS_MIXED || !b->view.tma))
-        return fail(CNS_ERR_INVALID, "the TMA assembly serves mixed-precision boxes with tensor maps only");
+    if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA && kernel != CNS_ASSEMBLE_TMA_WS)
+        return fail(CNS_ERR_INVALID, "unknown kernel %d", kernel);
+    if (kernel != CNS_ASSEMBLE_DIRECT && (b->desc.precision != CNS_MIXED || !b->view.tma))
+        return fail(CNS_ERR_INVALID, "the TMA assemblies serve mixed-precision boxes with tensor maps only");
     if (kernel == b->kernel) return CNS_OK;
     CK(cudaStreamSynchronize(b->stream));
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
@@ -1240,7 +1252,7 @@ extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], in
     BoxScalars hs;
     int rc = save_state(b, &hs);
     if (rc) return rc;
-    const int nkern = (b->desc.precision == CNS_MIXED && b->view.tma) ? 2 : 1;
+    const int nkern = (b->desc.precision == CNS_MIXED && b->view.tma) ? 3 : 1;
     int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]}, best_k = b->kernel;
     double best_t = 1e300;
     for (int c = -1; c < nkern * kNumShapes; c++) {  // c = -1: a warm-up trial, not scored
@@ -1304,7 +1316,7 @@ extern "C" int cns_batch_autotune(cns_batch* bt, int trial_steps, int* chosen_po
     };
     bool any_tma = false;
     for (auto* b : bt->members) any_tma = any_tma || (b->desc.precision == CNS_MIXED && b->view.tma);
-    const int npolicies = (kNumShapes + 1) * (any_tma ? 2 : 1);
+    const int npolicies = (kNumShapes + 1) * (any_tma ? 3 : 1);
     int best = 0;
     double best_t = 1e300;
     for (int policy = -1; policy < npolicies; policy++) {  // -1: warm-up with policy 0

@@ -21,6 +21,9 @@ size_t tma_maps_bytes();
 cudaError_t tma_encode_maps(const BoxView& v, void* out);
 cudaError_t bounded_wait_selftest(int* status);
 cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
+// the warp-specialised TMA assembly (same tiles, same bits): stencils and FP64 write-back overlap
+cudaError_t launch_assemble_ws(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
+bool assemble_ws_fits();  // its 512-thread, 160 KB block fits on the current device
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st);
 
 // operator-level kernels and layout conversions (cns_ops.cu)

@@ -52,6 +52,12 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)_
 __device__ __forceinline__ void mbar_init(uint64_t* bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
 }
+__device__ __forceinline__ void mbar_init_n(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
@@ -196,6 +202,258 @@ __device__ __forceinline__ void lap_full(const float* s, int tj, int tk, float c
     }
 }
 
+// The sums of one tile, per thread (its 8 cells along i): f0..f4 of the five conserved
+// variables (f1..f4 accumulate in dmx, dmy, dmz, de) and the centre velocity c0.
+
+// Field e of a tile's 20 loads (schedule kSched), staged at s, folded into the sums.
+__device__ __forceinline__ void consume_field(int e, const float* s, const Tile& T, const BoxView& b,
+                                              const CoefT<float>& cf, int tj, int tk, float* dmx, float* dmy,
+                                              float* dmz, float* de, float* f0, float* c0) {
+    switch (e) {
+        case 0: {  // SPHI: de starts from eta * Phi
+            using B = Bx<BX_C>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) de[i] = s[B::at(i, tj, tk)];
+            break;
+        }
+        case 1: {  // PT: de = tc T0 + phi, then the x, y, z second differences
+            float t0[XI];
+            lap_full(s, tj, tk, cf.tc, cf.tl[0], cf.tl[1], cf.tl[2], de, t0, true);
+            break;
+        }
+        case 2:  // PU: dmx = vc0 u0 + x, y, z second differences
+            lap_full(s, tj, tk, cf.vc[0], cf.vl[0][0], cf.vl[0][1], cf.vl[0][2], dmx, c0, false);
+            break;
+        case 3: {  // SX: dmx += (eta/3) d/dx (v_y + w_z); then the work term dmx u0
+            using B = Bx<BX_I>;
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmx[i] = cd1acc(dmx[i], col, i + 4, cf.mx[0]);
+                de[i] = fmaf(dmx[i], c0[i], de[i]);
+            }
+            break;
+        }
+        case 4:
+            lap_full(s, tj, tk, cf.vc[1], cf.vl[1][0], cf.vl[1][1], cf.vl[1][2], dmy, c0, false);
+            break;
+        case 5: {  // SY
+            using B = Bx<BX_J>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
+                de[i] = fmaf(dmy[i], c0[i], de[i]);
+            }
+            break;
+        }
+        case 6:
+            lap_full(s, tj, tk, cf.vc[2], cf.vl[2][0], cf.vl[2][1], cf.vl[2][2], dmz, c0, false);
+            break;
+        case 7: {  // SZ
+            using B = Bx<BX_K>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.mx[2]);
+                de[i] = fmaf(dmz[i], c0[i], de[i]);
+            }
+            break;
+        }
+        case 8: {  // PMX: f0 = -d(rho u)/dx
+            using B = Bx<BX_I>;
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) f0[i] = cd1(col, i + 4, cf.ha[0]);
+            break;
+        }
+        case 9: {  // PMY
+            using B = Bx<BX_J>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+            break;
+        }
+        case 10: {  // PMZ
+            using B = Bx<BX_K>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+            break;
+        }
+        case 11: {  // PFUU along x -> f1 (in dmx)
+            using B = Bx<BX_I>;
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) dmx[i] = cd1acc(dmx[i], col, i + 4, cf.ha[0]);
+            break;
+        }
+        case 12: {  // PFUV: along y -> f1, along x -> f2 (in dmy)
+            using B = Bx<BX_IJ>;
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj + 4, tk), B::K, cf.ha[1]);
+                dmy[i] = cd1acc(dmy[i], col, i + 4, cf.ha[0]);
+            }
+            break;
+        }
+        case 13: {  // PFUW: along z -> f1, along x -> f3 (in dmz)
+            using B = Bx<BX_IK>;
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk + 4)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj, tk + 4), 1, cf.ha[2]);
+                dmz[i] = cd1acc(dmz[i], col, i + 4, cf.ha[0]);
+            }
+            break;
+        }
+        case 14: {  // PFVV along y -> f2
+            using B = Bx<BX_J>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+            break;
+        }
+        case 15: {  // PFVW: along z -> f2, along y -> f3
+            using B = Bx<BX_JK>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                const float* p = s + B::at(i, tj + 4, tk + 4);
+                dmy[i] = sd1acc(dmy[i], p, 1, cf.ha[2]);
+                dmz[i] = sd1acc(dmz[i], p, B::K, cf.ha[1]);
+            }
+            break;
+        }
+        case 16: {  // PFWW along z -> f3
+            using B = Bx<BX_K>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+            break;
+        }
+        case 17: {  // PHU along x -> f4 (in de)
+            using B = Bx<BX_I>;
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) de[i] = cd1acc(de[i], col, i + 4, cf.ha[0]);
+            break;
+        }
+        case 18: {  // PHV
+            using B = Bx<BX_J>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+            break;
+        }
+        default: {  // 19, PHW; then -H_ref div(u) (the P set holds ((E+p) - H_ref) u), with
+                   // div(u) = (S_x + S_y + S_z) / 2 read at the cell (S is L2-resident)
+            using B = Bx<BX_K>;
+            const float href = -(float)b.sc->H_ref;
+            const float* S = (const float*)b.S;
+            const int j = min(T.j0 + tj, b.n[1] - 1), k = min(T.k0 + tk, b.n[2] - 1);
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                const long long c = cell_off(b, min(T.i0 + i, b.n[0] - 1), j, k);
+                const float hsum = __ldg(S + SX * b.fs + c) + __ldg(S + SY * b.fs + c) + __ldg(S + SZ * b.fs + c);
+                const float a = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                de[i] = fmaf(href, 0.5f * hsum, a);
+            }
+            break;
+        }
+    }
+}
+
+// Park the five sums of a thread's 8 cells at column `col` of a 40 KB stash; the write-back
+// reads them back as stash[(i * 5 + l) * 256 + col].
+__device__ __forceinline__ void park_sums(float* stash, int col, const float* f0, const float* dmx, const float* dmy,
+                                          const float* dmz, const float* de) {
+#pragma unroll
+    for (int i = 0; i < XI; i++) {
+        stash[(i * 5 + 0) * kTileThreads + col] = f0[i];
+        stash[(i * 5 + 1) * kTileThreads + col] = dmx[i];
+        stash[(i * 5 + 2) * kTileThreads + col] = dmy[i];
+        stash[(i * 5 + 3) * kTileThreads + col] = dmz[i];
+        stash[(i * 5 + 4) * kTileThreads + col] = de[i];
+    }
+}
+
+// RK3 stage combine (FP64) and the fused write-back, as in k_assemble, of the 8 cells of
+// column `col` = (tj, tk) of tile T whose sums are parked in `stash`; health bits and (stage 3)
+// the Courant number folded into the box's scalars.  Every lane of the calling warp takes part.
+template <int STAGE>
+__device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, const float* stash, int col, int tj,
+                                           int tk) {
+    const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
+    float* Pw = (float*)b.P[pr ^ 1];
+    const double dt = b.sc->dt;
+    const MixedRefs refs = mixed_refs(b);
+    const int j = T.j0 + tj, k = T.k0 + tk;
+    const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
+    const long long fs = b.fs;
+    double cmax = 0.0;
+    int health = 0;
+    // Software-pipelined: the state of cell i + 1 is loaded while cell i is computed (the
+    // loads of cells outside the box are clamped to a cell inside it and never used).
+    double nu[5], ns[5];
+    {
+        const long long c = cell_off(b, min(T.i0, b.n[0] - 1), jc, kc);
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+            nu[l] = b.U[c + l * fs];
+            ns[l] = STAGE == 1 ? 0.0 : b.Us[c + l * fs];
+        }
+    }
+#pragma unroll 2
+    for (int i = 0; i < XI; i++) {
+        double u0[5], us[5];
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+            u0[l] = nu[l];
+            us[l] = ns[l];
+        }
+        if (i + 1 < XI) {
+            const long long c1 = cell_off(b, min(T.i0 + i + 1, b.n[0] - 1), jc, kc);
+#pragma unroll
+            for (int l = 0; l < 5; l++) {
+                nu[l] = b.U[c1 + l * fs];
+                ns[l] = STAGE == 1 ? 0.0 : b.Us[c1 + l * fs];
+            }
+        }
+        const int ic = T.i0 + i;
+        if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+        const long long c = cell_off(b, ic, j, k);
+        float f[5];
+#pragma unroll
+        for (int l = 0; l < 5; l++) f[l] = stash[(i * 5 + l) * kTileThreads + col];
+        double un[5];
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+            const long long e = c + l * fs;
+            const double r = (double)f[l];
+            if (STAGE == 1) {
+                un[l] = fma(dt, r, u0[l]);
+                b.Us[e] = un[l];
+            } else if (STAGE == 2) {
+                un[l] = fma(0.75, u0[l], 0.25 * fma(dt, r, us[l]));
+                b.Us[e] = un[l];
+            } else {
+                un[l] = fma(1.0 / 3.0, u0[l], (2.0 / 3.0) * fma(dt, r, us[l]));
+                b.U[e] = un[l];
+            }
+        }
+        const double cour = epilogue_mixed(b, Pw, c, ic, j, k, un, STAGE == 3, &health, refs);
+        cmax = cour > cmax ? cour : cmax;
+    }
+    if (health) atomicOr(&b.sc->status, health);
+    if (STAGE == 3) courant_fold(b, cmax);
+}
+
 template <int STAGE>
 __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView* __restrict__ boxes,
                                                                const Tile* __restrict__ tiles, int ntiles) {
@@ -242,244 +500,128 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
                 }
                 return;
             }
-            const float* s = buf[g & 1];
-            switch (e) {
-                case 0: {  // SPHI: de starts from eta * Phi
-                    using B = Bx<BX_C>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) de[i] = s[B::at(i, tj, tk)];
-                    break;
-                }
-                case 1: {  // PT: de = tc T0 + phi, then the x, y, z second differences
-                    float t0[XI];
-                    lap_full(s, tj, tk, cf.tc, cf.tl[0], cf.tl[1], cf.tl[2], de, t0, true);
-                    break;
-                }
-                case 2:  // PU: dmx = vc0 u0 + x, y, z second differences
-                    lap_full(s, tj, tk, cf.vc[0], cf.vl[0][0], cf.vl[0][1], cf.vl[0][2], dmx, c0, false);
-                    break;
-                case 3: {  // SX: dmx += (eta/3) d/dx (v_y + w_z); then the work term dmx u0
-                    using B = Bx<BX_I>;
-                    float col[16];
-#pragma unroll
-                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        dmx[i] = cd1acc(dmx[i], col, i + 4, cf.mx[0]);
-                        de[i] = fmaf(dmx[i], c0[i], de[i]);
-                    }
-                    break;
-                }
-                case 4:
-                    lap_full(s, tj, tk, cf.vc[1], cf.vl[1][0], cf.vl[1][1], cf.vl[1][2], dmy, c0, false);
-                    break;
-                case 5: {  // SY
-                    using B = Bx<BX_J>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
-                        de[i] = fmaf(dmy[i], c0[i], de[i]);
-                    }
-                    break;
-                }
-                case 6:
-                    lap_full(s, tj, tk, cf.vc[2], cf.vl[2][0], cf.vl[2][1], cf.vl[2][2], dmz, c0, false);
-                    break;
-                case 7: {  // SZ
-                    using B = Bx<BX_K>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.mx[2]);
-                        de[i] = fmaf(dmz[i], c0[i], de[i]);
-                    }
-                    break;
-                }
-                case 8: {  // PMX: f0 = -d(rho u)/dx
-                    using B = Bx<BX_I>;
-                    float col[16];
-#pragma unroll
-                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
-#pragma unroll
-                    for (int i = 0; i < XI; i++) f0[i] = cd1(col, i + 4, cf.ha[0]);
-                    break;
-                }
-                case 9: {  // PMY
-                    using B = Bx<BX_J>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
-                    break;
-                }
-                case 10: {  // PMZ
-                    using B = Bx<BX_K>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
-                    break;
-                }
-                case 11: {  // PFUU along x -> f1 (in dmx)
-                    using B = Bx<BX_I>;
-                    float col[16];
-#pragma unroll
-                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
-#pragma unroll
-                    for (int i = 0; i < XI; i++) dmx[i] = cd1acc(dmx[i], col, i + 4, cf.ha[0]);
-                    break;
-                }
-                case 12: {  // PFUV: along y -> f1, along x -> f2 (in dmy)
-                    using B = Bx<BX_IJ>;
-                    float col[16];
-#pragma unroll
-                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk)];
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj + 4, tk), B::K, cf.ha[1]);
-                        dmy[i] = cd1acc(dmy[i], col, i + 4, cf.ha[0]);
-                    }
-                    break;
-                }
-                case 13: {  // PFUW: along z -> f1, along x -> f3 (in dmz)
-                    using B = Bx<BX_IK>;
-                    float col[16];
-#pragma unroll
-                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk + 4)];
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj, tk + 4), 1, cf.ha[2]);
-                        dmz[i] = cd1acc(dmz[i], col, i + 4, cf.ha[0]);
-                    }
-                    break;
-                }
-                case 14: {  // PFVV along y -> f2
-                    using B = Bx<BX_J>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
-                    break;
-                }
-                case 15: {  // PFVW: along z -> f2, along y -> f3
-                    using B = Bx<BX_JK>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        const float* p = s + B::at(i, tj + 4, tk + 4);
-                        dmy[i] = sd1acc(dmy[i], p, 1, cf.ha[2]);
-                        dmz[i] = sd1acc(dmz[i], p, B::K, cf.ha[1]);
-                    }
-                    break;
-                }
-                case 16: {  // PFWW along z -> f3
-                    using B = Bx<BX_K>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
-                    break;
-                }
-                case 17: {  // PHU along x -> f4 (in de)
-                    using B = Bx<BX_I>;
-                    float col[16];
-#pragma unroll
-                    for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
-#pragma unroll
-                    for (int i = 0; i < XI; i++) de[i] = cd1acc(de[i], col, i + 4, cf.ha[0]);
-                    break;
-                }
-                case 18: {  // PHV
-                    using B = Bx<BX_J>;
-#pragma unroll
-                    for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
-                    break;
-                }
-                default: {  // 19, PHW; then -H_ref div(u) (the P set holds ((E+p) - H_ref) u), with
-                           // div(u) = (S_x + S_y + S_z) / 2 read at the cell (S is L2-resident)
-                    using B = Bx<BX_K>;
-                    const float href = -(float)b.sc->H_ref;
-                    const float* S = (const float*)b.S;
-                    const int j = min(T.j0 + tj, b.n[1] - 1), k = min(T.k0 + tk, b.n[2] - 1);
-#pragma unroll
-                    for (int i = 0; i < XI; i++) {
-                        const long long c = cell_off(b, min(T.i0 + i, b.n[0] - 1), j, k);
-                        const float hsum = __ldg(S + SX * b.fs + c) + __ldg(S + SY * b.fs + c) + __ldg(S + SZ * b.fs + c);
-                        const float a = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
-                        de[i] = fmaf(href, 0.5f * hsum, a);
-                    }
-                    break;
-                }
-            }
+            consume_field(e, buf[g & 1], T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
             __syncthreads();  // buffer g & 1 is free for load g + 2
         }
-        // RK3 stage combine (FP64) and the fused write-back, as in k_assemble.  The five sums
-        // of this thread's 8 cells are parked in the buffer the last field used (free: every
-        // thread passed the barrier after consuming it; each thread reads back only its own
-        // entries), so the write-back runs as a rolled loop and its code exists once, not 8x.
+        // The sums are parked in the buffer the last field used (free: every thread passed the
+        // barrier after consuming it; each thread reads back only its own entries), so the
+        // write-back runs as a rolled loop and its code exists once, not 8x.
         float* stash = buf[(g - 1) & 1];
-#pragma unroll
-        for (int i = 0; i < XI; i++) {
-            stash[(i * 5 + 0) * kTileThreads + tid] = f0[i];
-            stash[(i * 5 + 1) * kTileThreads + tid] = dmx[i];
-            stash[(i * 5 + 2) * kTileThreads + tid] = dmy[i];
-            stash[(i * 5 + 3) * kTileThreads + tid] = dmz[i];
-            stash[(i * 5 + 4) * kTileThreads + tid] = de[i];
-        }
-        const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
-        float* Pw = (float*)b.P[pr ^ 1];
-        const double dt = b.sc->dt;
-        const MixedRefs refs = mixed_refs(b);
-        const int j = T.j0 + tj, k = T.k0 + tk;
-        const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
-        const long long fs = b.fs;
-        double cmax = 0.0;
-        int health = 0;
-        // Software-pipelined: the state of cell i + 1 is loaded while cell i is computed (the
-        // loads of cells outside the box are clamped to a cell inside it and never used).
-        double nu[5], ns[5];
-        {
-            const long long c = cell_off(b, min(T.i0, b.n[0] - 1), jc, kc);
-#pragma unroll
-            for (int l = 0; l < 5; l++) {
-                nu[l] = b.U[c + l * fs];
-                ns[l] = STAGE == 1 ? 0.0 : b.Us[c + l * fs];
-            }
-        }
-#pragma unroll 2
-        for (int i = 0; i < XI; i++) {
-            double u0[5], us[5];
-#pragma unroll
-            for (int l = 0; l < 5; l++) {
-                u0[l] = nu[l];
-                us[l] = ns[l];
-            }
-            if (i + 1 < XI) {
-                const long long c1 = cell_off(b, min(T.i0 + i + 1, b.n[0] - 1), jc, kc);
-#pragma unroll
-                for (int l = 0; l < 5; l++) {
-                    nu[l] = b.U[c1 + l * fs];
-                    ns[l] = STAGE == 1 ? 0.0 : b.Us[c1 + l * fs];
-                }
-            }
-            const int ic = T.i0 + i;
-            if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
-            const long long c = cell_off(b, ic, j, k);
-            float f[5];
-#pragma unroll
-            for (int l = 0; l < 5; l++) f[l] = stash[(i * 5 + l) * kTileThreads + tid];
-            double un[5];
-#pragma unroll
-            for (int l = 0; l < 5; l++) {
-                const long long e = c + l * fs;
-                const double r = (double)f[l];
-                if (STAGE == 1) {
-                    un[l] = fma(dt, r, u0[l]);
-                    b.Us[e] = un[l];
-                } else if (STAGE == 2) {
-                    un[l] = fma(0.75, u0[l], 0.25 * fma(dt, r, us[l]));
-                    b.Us[e] = un[l];
-                } else {
-                    un[l] = fma(1.0 / 3.0, u0[l], (2.0 / 3.0) * fma(dt, r, us[l]));
-                    b.U[e] = un[l];
-                }
-            }
-            const double cour = epilogue_mixed(b, Pw, c, ic, j, k, un, STAGE == 3, &health, refs);
-            cmax = cour > cmax ? cour : cmax;
-        }
-        if (health) atomicOr(&b.sc->status, health);
-        if (STAGE == 3) courant_fold(b, cmax);
+        park_sums(stash, tid, f0, dmx, dmy, dmz, de);
+        write_back<STAGE>(b, T, stash, tid, tj, tk);
         __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
+    }
+}
+
+// ---- warp-specialised variant ------------------------------------------------------------
+// One 512-thread block per SM: warps 0-7 (the stencil group) run the 20 TMA-fed field phases of
+// tile t while warps 8-15 (the write-back group) run the FP64 write-back of tile t-1, so the
+// FP32 stencils and the FP64 write-back overlap instead of alternating.  The sums move between
+// the groups through two 40 KB stash slots: full[s] (256 stencil arrivals) hands slot s to the
+// write-back group, empty[s] (256 write-back arrivals) hands it back.  The stencil group
+// synchronises on named barrier 1 only; the write-back group needs no barrier.  Every wait is
+// bounded; a group that gives up sets HEALTH_TIMEOUT and returns, and the other group's next
+// wait then gives up too.  Same arithmetic as k_assemble_tma, same bits.
+constexpr int kWsThreads = 2 * kTileThreads;
+constexpr int kStashElems = 5 * XI * kTileThreads;  // 10240 floats
+static_assert(kStashElems == kBufElems, "a stash slot is one field buffer in size");
+
+__device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+// true on every thread of the stencil group if `p` holds on any of them
+__device__ __forceinline__ bool group_any(bool p) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred a, q;\n setp.ne.u32 a, %1, 0;\n bar.red.or.pred q, 1, 256, a;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)p)
+        : "memory");
+    return r != 0;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __restrict__ boxes,
+                                                            const Tile* __restrict__ tiles, int ntiles) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* buf = (float*)smem_raw;                          // 2 field buffers
+    float* stash = buf + 2 * kBufElems;                     // 2 stash slots
+    uint64_t* bar = (uint64_t*)(stash + 2 * kStashElems);   // TMA[2], full[2], empty[2]
+    uint64_t* full = bar + 2;
+    uint64_t* empty = bar + 4;
+    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    if (my_tiles <= 0) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        for (int q = 0; q < 2; q++) {
+            mbar_init_n(&full[q], kTileThreads);
+            mbar_init_n(&empty[q], kTileThreads);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    constexpr int flip = (STAGE - 1) & 1;
+
+    if (threadIdx.x >= kTileThreads) {  // ---- write-back group
+        const int wt = threadIdx.x - kTileThreads, tk = wt & (XK - 1), tj = wt >> 5;
+        for (int it = 0; it < my_tiles; it++) {
+            const Tile T = tiles[blockIdx.x + it * gridDim.x];
+            const BoxView& b = boxes[T.box];
+            const int slot = it & 1;
+            const bool ok = mbar_wait_bounded(&full[slot], (uint32_t)((it >> 1) & 1));
+            if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform, so the shuffles below stay whole
+                if ((wt & 31) == 0) atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                return;
+            }
+            write_back<STAGE>(b, T, stash + slot * kStashElems, wt, tj, tk);
+            mbar_arrive(&empty[slot]);
+        }
+        return;
+    }
+
+    // ---- stencil group
+    const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
+    const int total = my_tiles * kLoads;
+    if (tid == 0) issue(boxes, tiles, blockIdx.x, 0, flip, buf, &bar[0]);
+    float dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
+    int g = 0;
+    for (int it = 0; it < my_tiles; it++) {
+        const Tile T = tiles[blockIdx.x + it * gridDim.x];
+        const BoxView& b = boxes[T.box];
+        const CoefT<float>& cf = b.c32;
+        prefetch_state_l2(b, T, STAGE, tid);
+#pragma unroll
+        for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.f;
+        for (int e = 0; e < kLoads; e++, g++) {
+            if (tid == 0 && g + 1 < total) {
+                const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
+                issue(boxes, tiles, nt, (g + 1) % kLoads, flip, buf + ((g + 1) & 1) * kBufElems, &bar[(g + 1) & 1]);
+            }
+            const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+            if (group_any(!ok)) {
+                if (tid == 0) {
+                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                    mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+                    if (g + 1 < total) mbar_wait_bounded(&bar[(g + 1) & 1], (uint32_t)(((g + 1) >> 1) & 1));
+                }
+                return;
+            }
+            consume_field(e, buf + (g & 1) * kBufElems, T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
+            group_sync();  // buffer g & 1 is free for load g + 2
+        }
+        // hand the sums over: slot it & 1, once the write-back of tile it - 2 has released it
+        const int slot = it & 1;
+        if (it >= 2) {
+            const bool ok = mbar_wait_bounded(&empty[slot], (uint32_t)(((it >> 1) - 1) & 1));
+            if (group_any(!ok)) {
+                if (tid == 0) {
+                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                    if (g < total) mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));  // the copy in flight
+                }
+                return;
+            }
+        }
+        park_sums(stash + slot * kStashElems, tid, f0, dmx, dmy, dmz, de);
+        mbar_arrive(&full[slot]);
     }
 }
 
@@ -581,6 +723,43 @@ cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int nti
     if (stage == 1) return launch_tma_stage<1>(boxes, tiles, ntiles, st);
     if (stage == 2) return launch_tma_stage<2>(boxes, tiles, ntiles, st);
     return launch_tma_stage<3>(boxes, tiles, ntiles, st);
+}
+
+constexpr size_t kWsSmem = (2 * kBufElems + 2 * kStashElems) * sizeof(float) + 6 * sizeof(uint64_t);
+
+template <int STAGE>
+static cudaError_t launch_ws_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
+    auto fn = k_assemble_ws<STAGE>;
+    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kWsThreads, kWsSmem);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;  // 512 threads x 128 registers and 160 KB must fit
+    const int grid = ntiles < nsm * per ? ntiles : nsm * per;
+    fn<<<grid, kWsThreads, kWsSmem, st>>>(boxes, tiles, ntiles);
+    return cudaGetLastError();
+}
+
+bool assemble_ws_fits() {
+    int per = 0;
+    if (cudaFuncSetAttribute((const void*)k_assemble_ws<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsSmem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)k_assemble_ws<3>, kWsThreads, kWsSmem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return per >= 1;
+}
+
+cudaError_t launch_assemble_ws(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (stage == 1) return launch_ws_stage<1>(boxes, tiles, ntiles, st);
+    if (stage == 2) return launch_ws_stage<2>(boxes, tiles, ntiles, st);
+    return launch_ws_stage<3>(boxes, tiles, ntiles, st);
 }
 
 }  // namespace cns

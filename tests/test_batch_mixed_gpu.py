@@ -154,12 +154,18 @@ def test_autotune_keeps_results_and_state(gpu, cns):
     assert np.array_equal(box.download(), other.download())
 
 
-@pytest.mark.parametrize("n", [(19, 23, 37), (8, 8, 32), (33, 17, 40), (64, 64, 64)])
-def test_tma_assembly_equals_direct_bitwise(gpu, cns, n):
-    """The TMA-staged assembly and the direct one do the same arithmetic in the same order."""
+KERNELS = ("CNS_ASSEMBLE_DIRECT", "CNS_ASSEMBLE_TMA", "CNS_ASSEMBLE_TMA_WS")
+
+
+# (128, 128, 128) and (96, 80, 128): 1024 and 480 TMA tiles, several per block, so the
+# warp-specialised kernel reuses both stash slots and flips every barrier's parity.
+@pytest.mark.parametrize("n", [(19, 23, 37), (8, 8, 32), (33, 17, 40), (64, 64, 64), (96, 80, 128), (128, 128, 128)])
+def test_tma_assemblies_equal_direct_bitwise(gpu, cns, n):
+    """The TMA-staged assemblies and the direct one do the same arithmetic in the same order."""
     U0 = I.initial_state(n, perturb=1e-3, seed=17)
     out = []
-    for kern in (cns.CNS_ASSEMBLE_DIRECT, cns.CNS_ASSEMBLE_TMA):
+    for name in KERNELS:
+        kern = getattr(cns, name)
         b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=cns.CNS_MIXED)
         b.set_kernel(kern)
         assert b.kernel() == kern
@@ -168,7 +174,37 @@ def test_tma_assembly_equals_direct_bitwise(gpu, cns, n):
         b.sync()
         out.append(b.download())
         b.close()
-    assert np.array_equal(out[0], out[1])
+    for name, o in zip(KERNELS[1:], out[1:]):
+        assert np.array_equal(out[0], o), name
+
+
+def test_batched_boxes_on_every_assembly_kernel_match(gpu, cns):
+    """Mixed boxes batched on each assembly kernel (one kernel per batch, and all three in one
+    batch) give the same bits as on the direct kernel."""
+    sizes = [(40, 24, 72), (64, 64, 64), (20, 36, 33)]
+    U0 = [I.initial_state(n, perturb=1e-3, seed=30 + q) for q, n in enumerate(sizes)]
+
+    def run(kernels):
+        bt = cns.Batch()
+        boxes = []
+        for n, u, k in zip(sizes, U0, kernels):
+            b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=cns.CNS_MIXED)
+            b.set_kernel(getattr(cns, k))
+            b.upload(u)
+            bt.add(b)
+            boxes.append(b)
+        bt.advance(3)
+        bt.sync()
+        res = [b.download() for b in boxes]
+        bt.close()
+        for b in boxes:
+            b.close()
+        return res
+
+    ref = run([KERNELS[0]] * 3)
+    for ks in ([KERNELS[1]] * 3, [KERNELS[2]] * 3, list(KERNELS)):
+        for a, r in zip(run(ks), ref):
+            assert np.array_equal(a, r), ks
 
 
 def test_tma_kernel_refused_for_fp64_boxes(gpu, cns):
@@ -176,3 +212,5 @@ def test_tma_kernel_refused_for_fp64_boxes(gpu, cns):
     assert b.kernel() == cns.CNS_ASSEMBLE_DIRECT
     with pytest.raises(cns.CnsError):
         b.set_kernel(cns.CNS_ASSEMBLE_TMA)
+    with pytest.raises(cns.CnsError):
+        b.set_kernel(cns.CNS_ASSEMBLE_TMA_WS)
