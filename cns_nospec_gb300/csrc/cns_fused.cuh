@@ -151,9 +151,41 @@ __device__ __forceinline__ MixedRefs mixed_refs(const BoxView& b) {
     return {sc.p_ref, sc.e_ref, sc.E_ref};
 }
 
+// The mixed form's Courant number of a cell, in FP64: it sets dt, and an FP32 dt would advance
+// the mixed form by a different time each step (a drift of ~1e-7 dt per step that dominated
+// its error against FP64).  1/rho by one Newton step from the FP32 reciprocal (~1e-14).
+__device__ __forceinline__ double courant_mixed(const BoxView& b, double rho, double mx, double my, double mz,
+                                                double p) {
+    const double r64 = (double)(1.0f / (float)rho);
+    const double rinv = fma(r64, fma(-rho, r64, 1.0), r64);
+    const double cs = sqrt((kGamma * p) * rinv);
+    const double cx = (cs + fabs(mx) * rinv) * b.c64.cour[0];
+    const double cy = (cs + fabs(my) * rinv) * b.c64.cour[1];
+    const double cz = (cs + fabs(mz) * rinv) * b.c64.cour[2];
+    return fmax(fmax(cx, cy), cz);
+}
+
+// An FP32 estimate of courant_mixed from the FP32 reciprocal rf = 1/(float)rho, the FP32
+// velocities u = (float)m * rf and p32 = (float)p.  Counting 2^-24 per rounding (rho, 1/rho,
+// 1.4, p, two products, sqrt, |u|, the sum, 1/dx, the last product), its relative distance from
+// courant_mixed is at most ~7 * 2^-24 for states whose values are normal FP32 numbers.
+__device__ __forceinline__ float courant_mixed_est(const BoxView& b, float rf, float u, float v, float w, float p32) {
+    const float cs = sqrtf(1.4f * p32 * rf);
+    const float cx = (cs + fabsf(u)) * b.c32.cour[0];
+    const float cy = (cs + fabsf(v)) * b.c32.cour[1];
+    const float cz = (cs + fabsf(w)) * b.c32.cour[2];
+    return fmaxf(fmaxf(cx, cy), cz);
+}
+
+// What a write-back that defers the FP64 Courant number keeps of a cell: the estimate and p.
+struct CourantInput {
+    float est;
+    double p;
+};
+
 __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
                                                  int k, const double un[5], bool want_cour, int* health,
-                                                 const MixedRefs& sc);
+                                                 const MixedRefs& sc, CourantInput* ci = nullptr);
 template <>
 __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __restrict__ Pw, long long c, int i,
                                                   int j, int k, const double un[5], bool want_cour, int* health) {
@@ -161,7 +193,7 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
 }
 __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
                                                  int k, const double un[5], bool want_cour, int* health,
-                                                 const MixedRefs& sc) {
+                                                 const MixedRefs& sc, CourantInput* ci) {
     const long long fs = b.fs;
     const double rho = un[0], E = un[4];
     const float rhof = (float)rho;
@@ -196,16 +228,12 @@ __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __rest
     store_img(Pw + PHU * fs, b, c, i, j, k, dH * u, 1);
     store_img(Pw + PHV * fs, b, c, i, j, k, dH * v, 2);
     store_img(Pw + PHW * fs, b, c, i, j, k, dH * w, 4);
+    if (ci) {
+        ci->p = pd + sc.p;
+        ci->est = courant_mixed_est(b, rf, u, v, w, (float)ci->p);
+    }
     if (!want_cour) return 0.0;
-    // The Courant number sets dt, and an FP32 dt would advance the mixed form by a different
-    // time each step (a drift of ~1e-7 dt per step that dominates its error against FP64).
-    // Formed in FP64 once per step: 1/rho by one Newton step from the FP32 seed (~1e-14).
-    const double rinv = fma(r64, fma(-rho, r64, 1.0), r64);
-    const double cs = sqrt((kGamma * (pd + sc.p)) * rinv);
-    const double cx = (cs + fabs(un[1]) * rinv) * b.c64.cour[0];
-    const double cy = (cs + fabs(un[2]) * rinv) * b.c64.cour[1];
-    const double cz = (cs + fabs(un[3]) * rinv) * b.c64.cour[2];
-    return fmax(fmax(cx, cy), cz);
+    return courant_mixed(b, rho, un[1], un[2], un[3], pd + sc.p);
 }
 
 // Warp max of positive doubles via their bit patterns; lane 0 folds it into the box max.

@@ -387,7 +387,7 @@ __device__ __forceinline__ void park_sums(float* stash, int col, const float* f0
 // column `col` = (tj, tk) of tile T whose sums are parked in `stash`; health bits and (stage 3)
 // the Courant number folded into the box's scalars.  Every lane of the calling warp takes part.
 template <int STAGE>
-__device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, const float* stash, int col, int tj,
+__device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, float* stash, int col, int tj,
                                            int tk) {
     const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
     float* Pw = (float*)b.P[pr ^ 1];
@@ -397,6 +397,7 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, cons
     const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
     const long long fs = b.fs;
     double cmax = 0.0;
+    float m32 = 0.0f;  // stage 3: the largest FP32 Courant estimate of this thread's cells
     int health = 0;
     // Software-pipelined: the state of cell i + 1 is loaded while cell i is computed (the
     // loads of cells outside the box are clamped to a cell inside it and never used).
@@ -447,11 +448,49 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, cons
                 b.U[e] = un[l];
             }
         }
-        const double cour = epilogue_mixed(b, Pw, c, ic, j, k, un, STAGE == 3, &health, refs);
-        cmax = cour > cmax ? cour : cmax;
+        if (STAGE == 3) {
+            // park the FP32 Courant estimate and p (FP64, as two words) over the cell's sums
+            CourantInput ci;
+            epilogue_mixed(b, Pw, c, ic, j, k, un, false, &health, refs, &ci);
+            stash[(i * 5 + 0) * kTileThreads + col] = ci.est;
+            stash[(i * 5 + 1) * kTileThreads + col] = __int_as_float(__double2hiint(ci.p));
+            stash[(i * 5 + 2) * kTileThreads + col] = __int_as_float(__double2loint(ci.p));
+            m32 = fmaxf(m32, ci.est);
+        } else {
+            epilogue_mixed(b, Pw, c, ic, j, k, un, false, &health, refs);
+        }
     }
     if (health) atomicOr(&b.sc->status, health);
-    if (STAGE == 3) courant_fold(b, cmax);
+    if (STAGE == 3) {
+        // The FP64 Courant number only of the cells that can hold this thread's maximum: with
+        // |est - exact| <= eps * exact (eps = 2^-20, 16x the estimate's error bound), a cell
+        // whose estimate is below (1 - 2 eps) of the largest estimate is below that cell's exact
+        // value, so the maximum over the candidates is the maximum over all cells, bit for bit.
+        // NaN or tiny estimates (outside the bound's range) are always candidates, and all cells
+        // are when an estimate overflowed.  The warp runs the FP64 code once per round of
+        // candidates (mostly one), not once per cell.
+        const float thr = m32 * (1.0f - 0x1p-18f);
+        const bool all = !(m32 <= 3.0e38f);
+        unsigned cand = 0;
+#pragma unroll
+        for (int i = 0; i < XI; i++) {
+            const float est = stash[(i * 5 + 0) * kTileThreads + col];
+            const bool inside = T.i0 + i < b.n[0] && j < b.n[1] && k < b.n[2];
+            if (inside && (all || !(est < thr) || !(est > 1e-30f))) cand |= 1u << i;
+        }
+        while (__any_sync(0xffffffffu, cand != 0)) {
+            if (cand) {
+                const int i = __ffs(cand) - 1;
+                cand &= cand - 1;
+                const long long c = cell_off(b, T.i0 + i, j, k);
+                const double p = __hiloint2double(__float_as_int(stash[(i * 5 + 1) * kTileThreads + col]),
+                                                  __float_as_int(stash[(i * 5 + 2) * kTileThreads + col]));
+                const double cour = courant_mixed(b, b.U[c], b.U[c + fs], b.U[c + 2 * fs], b.U[c + 3 * fs], p);
+                cmax = cour > cmax ? cour : cmax;
+            }
+        }
+        courant_fold(b, cmax);
+    }
 }
 
 template <int STAGE>
@@ -516,42 +555,37 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
 // ---- warp-specialised variant ------------------------------------------------------------
 // One 512-thread block per SM: warps 0-7 (the stencil group) run the 20 TMA-fed field phases of
 // tile t while warps 8-15 (the write-back group) run the FP64 write-back of tile t-1, so the
-// FP32 stencils and the FP64 write-back overlap instead of alternating.  The sums move between
-// the groups through two 40 KB stash slots: full[s] (256 stencil arrivals) hands slot s to the
+// FP32 stencils and the FP64 write-back overlap instead of alternating.  The fields are
+// double-buffered (a third buffer measured slower: 200 KB of shared memory leaves too little
+// L1).  The sums move between the
+// groups through two 40 KB stash slots: full[s] (256 stencil arrivals) hands slot s to the
 // write-back group, empty[s] (256 write-back arrivals) hands it back.  The stencil group
-// synchronises on named barrier 1 only; the write-back group needs no barrier.  Every wait is
-// bounded; a group that gives up sets HEALTH_TIMEOUT and returns, and the other group's next
-// wait then gives up too.  Same arithmetic as k_assemble_tma, same bits.
+// synchronises on named barrier 1 only (once per field); the write-back group needs no barrier.
+// Every wait is bounded.  A stencil thread whose wait gives up stops waiting and computing but
+// keeps taking part in the barrier and the hand-over, so no thread is ever left waiting on it;
+// it reports HEALTH_TIMEOUT at the end, after thread 0 has waited (bounded) for the copies it
+// issued.  A write-back warp whose wait gives up reports and returns.  Same arithmetic as
+// k_assemble_tma, same bits.
 constexpr int kWsThreads = 2 * kTileThreads;
 constexpr int kStashElems = 5 * XI * kTileThreads;  // 10240 floats
 static_assert(kStashElems == kBufElems, "a stash slot is one field buffer in size");
 
+constexpr int kWsBufs = 2;
 __device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-// true on every thread of the stencil group if `p` holds on any of them
-__device__ __forceinline__ bool group_any(bool p) {
-    uint32_t r;
-    asm volatile(
-        "{\n .reg .pred a, q;\n setp.ne.u32 a, %1, 0;\n bar.red.or.pred q, 1, 256, a;\n selp.u32 %0, 1, 0, q;\n}\n"
-        : "=r"(r)
-        : "r"((uint32_t)p)
-        : "memory");
-    return r != 0;
-}
 
 template <int STAGE>
 __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __restrict__ boxes,
                                                             const Tile* __restrict__ tiles, int ntiles) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* buf = (float*)smem_raw;                          // 2 field buffers
-    float* stash = buf + 2 * kBufElems;                     // 2 stash slots
-    uint64_t* bar = (uint64_t*)(stash + 2 * kStashElems);   // TMA[2], full[2], empty[2]
-    uint64_t* full = bar + 2;
-    uint64_t* empty = bar + 4;
+    float* buf = (float*)smem_raw;                                // kWsBufs field buffers
+    float* stash = buf + kWsBufs * kBufElems;                     // 2 stash slots
+    uint64_t* bar = (uint64_t*)(stash + 2 * kStashElems);         // TMA[kWsBufs], full[2], empty[2]
+    uint64_t* full = bar + kWsBufs;
+    uint64_t* empty = full + 2;
     const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     if (my_tiles <= 0) return;
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0]);
-        mbar_init(&bar[1]);
+        for (int q = 0; q < kWsBufs; q++) mbar_init(&bar[q]);
         for (int q = 0; q < 2; q++) {
             mbar_init_n(&full[q], kTileThreads);
             mbar_init_n(&empty[q], kTileThreads);
@@ -581,9 +615,17 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
     // ---- stencil group
     const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
     const int total = my_tiles * kLoads;
-    if (tid == 0) issue(boxes, tiles, blockIdx.x, 0, flip, buf, &bar[0]);
-    float dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
+    auto issue_load = [&](int l) {  // load l of this block into buffer l % kWsBufs
+        const int nt = blockIdx.x + (l / kLoads) * gridDim.x;
+        issue(boxes, tiles, nt, l % kLoads, flip, buf + (l % kWsBufs) * kBufElems, &bar[l % kWsBufs]);
+    };
+    int issued = 0;  // thread 0: loads issued so far
+    if (tid == 0)
+        for (; issued < kWsBufs - 1 && issued < total; issued++) issue_load(issued);
+    bool bad = false;
+    int* bad_status = nullptr;  // the status word of the box whose wait gave up
     int g = 0;
+    float dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
     for (int it = 0; it < my_tiles; it++) {
         const Tile T = tiles[blockIdx.x + it * gridDim.x];
         const BoxView& b = boxes[T.box];
@@ -592,36 +634,29 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
 #pragma unroll
         for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.f;
         for (int e = 0; e < kLoads; e++, g++) {
-            if (tid == 0 && g + 1 < total) {
-                const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
-                issue(boxes, tiles, nt, (g + 1) % kLoads, flip, buf + ((g + 1) & 1) * kBufElems, &bar[(g + 1) & 1]);
+            // buffer (g + kWsBufs - 1) % kWsBufs held load g - 1, consumed before the last barrier
+            if (tid == 0 && !bad && issued < total && issued <= g + kWsBufs - 1) issue_load(issued++);
+            if (!bad && !mbar_wait_bounded(&bar[g % kWsBufs], (uint32_t)((g / kWsBufs) & 1))) {
+                bad = true;
+                bad_status = &b.sc->status;
             }
-            const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
-            if (group_any(!ok)) {
-                if (tid == 0) {
-                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
-                    mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
-                    if (g + 1 < total) mbar_wait_bounded(&bar[(g + 1) & 1], (uint32_t)(((g + 1) >> 1) & 1));
-                }
-                return;
-            }
-            consume_field(e, buf + (g & 1) * kBufElems, T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
-            group_sync();  // buffer g & 1 is free for load g + 2
+            if (!bad) consume_field(e, buf + (g % kWsBufs) * kBufElems, T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
+            group_sync();  // buffer g % kWsBufs is free for load g + kWsBufs
         }
         // hand the sums over: slot it & 1, once the write-back of tile it - 2 has released it
         const int slot = it & 1;
-        if (it >= 2) {
-            const bool ok = mbar_wait_bounded(&empty[slot], (uint32_t)(((it >> 1) - 1) & 1));
-            if (group_any(!ok)) {
-                if (tid == 0) {
-                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
-                    if (g < total) mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));  // the copy in flight
-                }
-                return;
-            }
+        if (it >= 2 && !bad && !mbar_wait_bounded(&empty[slot], (uint32_t)(((it >> 1) - 1) & 1))) {
+            bad = true;
+            bad_status = &b.sc->status;
         }
         park_sums(stash + slot * kStashElems, tid, f0, dmx, dmy, dmz, de);
         mbar_arrive(&full[slot]);
+    }
+    if (bad) {
+        atomicOr(bad_status, HEALTH_TIMEOUT);
+        if (tid == 0)  // the copies still in flight are among the last ones issued
+            for (int l = max(0, issued - kWsBufs); l < issued; l++)
+                mbar_wait_bounded(&bar[l % kWsBufs], (uint32_t)((l / kWsBufs) & 1));
     }
 }
 
@@ -725,7 +760,7 @@ cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int nti
     return launch_tma_stage<3>(boxes, tiles, ntiles, st);
 }
 
-constexpr size_t kWsSmem = (2 * kBufElems + 2 * kStashElems) * sizeof(float) + 6 * sizeof(uint64_t);
+constexpr size_t kWsSmem = (kWsBufs * kBufElems + 2 * kStashElems) * sizeof(float) + (kWsBufs + 4) * sizeof(uint64_t);
 
 template <int STAGE>
 static cudaError_t launch_ws_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
