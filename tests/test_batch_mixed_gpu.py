@@ -178,6 +178,27 @@ def test_tma_assemblies_equal_direct_bitwise(gpu, cns, n):
         assert np.array_equal(out[0], o), name
 
 
+def test_courant_near_ties_equal_direct_bitwise(gpu, cns):
+    """A nearly uniform state (velocity amplitudes 1e-6, perturbation 1e-9): every cell's
+    Courant number ties with the maximum to within the FP32 estimate's error, so the TMA
+    kernels' exact-maximum search has to evaluate (almost) every cell in FP64; dt and the state
+    must still equal the direct kernel's bit for bit."""
+    n = (40, 36, 64)
+    U0 = I.initial_state(n, amp=(1e-6, 1e-6, 1e-6), perturb=1e-9, seed=23)
+    out = []
+    for name in KERNELS:
+        b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=cns.CNS_MIXED)
+        b.set_kernel(getattr(cns, name))
+        b.upload(U0)
+        b.advance(3)
+        b.sync()
+        out.append((b.download(), b.last_dt()))
+        b.close()
+    for name, (u, dt) in zip(KERNELS[1:], out[1:]):
+        assert dt == out[0][1], name
+        assert np.array_equal(u, out[0][0]), name
+
+
 def test_batched_boxes_on_every_assembly_kernel_match(gpu, cns):
     """Mixed boxes batched on each assembly kernel (one kernel per batch, and all three in one
     batch) give the same bits as on the direct kernel."""
