@@ -2,6 +2,7 @@
 // reference's host-array entry points, graphs and launch accounting.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -241,6 +242,7 @@ struct cns_box {
     int kernel = CNS_ASSEMBLE_DIRECT;  // which k_assemble a mixed box runs
     cudaGraphExec_t gexec = nullptr;
     cns_batch* batch = nullptr;
+    double* host_out = nullptr;  // the source of the device view's host_out (see set_host_out)
 };
 
 extern "C" long long cns_box_bytes(const cns_box_desc* desc) {
@@ -1003,11 +1005,36 @@ static int cached_box(const cns_box_desc& d, cns_box** out) {
 // Copy a host state in, fill its ghosts (the reference's fill_boundary at the start of the
 // step), run nsteps, and copy back the interior of the result with the ghosts of the last
 // step's start state -- what the reference leaves in U (cpu/advance.cpp:45,144-153).
+// Point the box's device view at a page-locked host array (or at nothing): stage 3 then also
+// stores every cell's new state there.  Stream-ordered; the pointer is copied from the box
+// itself, which outlives the copy.
+static int set_host_out(cns_box* b, double* h_map) {
+    b->host_out = h_map;
+    b->view.host_out = h_map;
+    CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, host_out), &b->host_out, sizeof(double*),
+                       cudaMemcpyHostToDevice, b->stream));
+    return CNS_OK;
+}
+
+// Clears the device view's host pointer when the call returns, on every path: no later launch
+// may write to the caller's memory after this call.
+struct HostOutGuard {
+    cns_box* b = nullptr;
+    ~HostOutGuard() {
+        if (b && b->host_out) {
+            set_host_out(b, nullptr);
+            cudaStreamSynchronize(b->stream);
+        }
+    }
+};
+
 static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt_hist) {
     cns_box* b;
     int rc = cached_box(d, &b);
     if (rc) return rc;
     double* h_map = (double*)mapped_host_range(U, aos_bytes(b));
+    HostOutGuard guard;
+    guard.b = b;
     // the last step's start state supplies the ghosts: with at most one step that is the input
     const bool ghosts_on_upload = h_map && nsteps <= 1;
     if ((rc = upload_host(b, U, h_map, ghosts_on_upload))) return rc;
@@ -1020,7 +1047,10 @@ static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt
                 CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
             else if (!ghosts_on_upload)
                 CK(host_ghosts(b->view, h_map, b->stream));
+            // in place: the last step's stage 3 writes the interior straight to the caller
+            if (h_map && (rc = set_host_out(b, h_map))) return rc;
             if ((rc = cns_box_advance(b, 1))) return rc;
+            if (h_map && (rc = set_host_out(b, nullptr))) return rc;
         } else if ((rc = cns_box_advance(b, chunk))) {
             return rc;
         }
@@ -1032,9 +1062,9 @@ static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt
         }
         done += chunk;
     }
-    if (h_map) {
-        if ((rc = download_host(b, U, h_map, false))) return rc;
-    } else {
+    // in place, the array is complete: ghosts written at upload or before the last step, the
+    // interior by the last stage 3 (or, with no step, the input itself)
+    if (!h_map) {
         if (nsteps == 0) CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
         if ((rc = download_host(b, U, nullptr, false))) return rc;
     }

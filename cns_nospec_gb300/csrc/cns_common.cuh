@@ -94,6 +94,9 @@ struct BoxView {
     void* S;                // NSF fields, precision R
     BoxScalars* sc;
     double* dtlog;          // dt of completed steps, ring of DTLOG_CAP entries
+    double* host_out;       // when set (only around the last step of a host-array call): the
+                            // device address of the caller's page-locked host array; stage 3
+                            // also stores each cell's new state there, in the reference layout
     const void* tma;        // mixed boxes: device copy of the TMA tensor maps of P[0], P[1], S
     double cfl;
     int precision;          // 0 = plain FP64, 1 = mixed

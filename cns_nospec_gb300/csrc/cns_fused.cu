@@ -165,6 +165,7 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
                     b.U[e] = un[l];
                 }
             }
+            if (STAGE == 3 && b.host_out) store_host(b, i, j, k, un);
             cour = epilogue<R>(b, Pw, c, i, j, k, un, STAGE == 3, &health);
         }
         if (health) atomicOr(&b.sc->status, health);

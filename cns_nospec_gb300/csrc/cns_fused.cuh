@@ -85,6 +85,16 @@ __device__ __forceinline__ void store_img(R* __restrict__ f, const BoxView& b, l
     }
 }
 
+// Stage 3 of a step whose result goes straight to the caller's page-locked host array
+// (BoxView::host_out): the cell's new state at U[i+4][j+4][k+4][0..4] of the reference layout,
+// written over the CPU-GPU link while the kernel computes.
+__device__ __forceinline__ void store_host(const BoxView& b, int i, int j, int k, const double un[5]) {
+    const long long g1 = b.n[1] + 2 * CNS_NG, g2 = b.n[2] + 2 * CNS_NG;
+    double* h = b.host_out + (((long long)(i + CNS_NG) * g1 + (j + CNS_NG)) * g2 + (k + CNS_NG)) * CNS_NC;
+#pragma unroll
+    for (int l = 0; l < CNS_NC; l++) h[l] = un[l];
+}
+
 // Health bits from raw IEEE fields (integer ops only; no FP64 pipe work).
 __device__ __forceinline__ int health_bits(double rho, double eint) {
     unsigned long long rb = dbits(rho), eb = dbits(eint);

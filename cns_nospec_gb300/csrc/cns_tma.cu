@@ -449,6 +449,7 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
             }
         }
         if (STAGE == 3) {
+            if (b.host_out) store_host(b, ic, j, k, un);
             // park the FP32 Courant estimate and p (FP64, as two words) over the cell's sums
             CourantInput ci;
             epilogue_mixed(b, Pw, c, ic, j, k, un, false, &health, refs, &ci);
