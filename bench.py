@@ -140,6 +140,11 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def box_workload(n):
+    """The name of the single-box workload, the same on both arms."""
+    return f"periodic box {n}^3 + 4 ghosts, FP64 RK3 step, sinusoidal field with a 1e-3 perturbation (seed 1)"
+
+
 def pinned_like(shape):
     """A pinned host float64 array when torch is importable (plumbing only), else pageable."""
     try:
@@ -215,7 +220,7 @@ def run_reference(args, dist):
     return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"periodic box {n}^3 + 4 ghosts, FP64 RK3 (cpu/ path algorithm)", "n": n,
+            "config": {"workload": box_workload(n), "n": n,
                        "host_threads": threads},
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind,
                              "sample": f"{steps} RK3 steps of the {n}^3 box on the host cores"},
@@ -321,7 +326,7 @@ def run_ours(args, dist):
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"periodic box {n}^3 + 4 ghosts, FP64 plain RK3 (config 1 field, seed 1)",
+        "config": {"workload": box_workload(n),
                    "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
                    "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
                    "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)},
@@ -439,7 +444,7 @@ def run_batch(args):
 
 
 def run_mixed256(args):
-    """256^3 box, config-1 field: FP64 and mixed forms, 100 RK3 steps each; normwise error
+    """256^3 box, the perturbed sinusoidal field: FP64 and mixed forms, 100 RK3 steps each; normwise error
     of the mixed form against FP64 per conserved variable, and cell-updates/s of both."""
     import cns_nospec_gb300 as C
     from cns_nospec_gb300 import _lib as L
@@ -457,7 +462,7 @@ def run_mixed256(args):
         out[prec] = b.download()
         b.close()
     mx, rms = I.normwise_error(out[C.CNS_MIXED], out[C.CNS_FP64])
-    return {"workload": f"periodic box {n}^3, config-1 field, {args.steps} RK3 steps", "fp64_cell_updates_per_s":
+    return {"workload": f"periodic box {n}^3, sinusoidal field with a 1e-3 perturbation (seed 1), {args.steps} RK3 steps", "fp64_cell_updates_per_s":
             rate[C.CNS_FP64], "mixed_cell_updates_per_s": rate[C.CNS_MIXED],
             "speedup": rate[C.CNS_MIXED] / rate[C.CNS_FP64], "max_normwise_err": [float(x) for x in mx],
             "rms_normwise_err": [float(x) for x in rms], "vars": ["rho", "rho u", "rho v", "rho w", "rho E"]}

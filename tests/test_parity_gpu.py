@@ -112,7 +112,7 @@ def test_advance_noncubic_matches_oracle(gpu, cns, oracle, n):
     assert np.allclose(dts, rdt, rtol=1e-13, atol=0)
 
 
-def test_advance_config1_128cube_100_steps(gpu, cns, oracle):
+def test_advance_perturbed_128cube_100_steps(gpu, cns, oracle):
     """128^3, perturbed field, 100 RK3 steps against the oracle run live."""
     n = 128
     U0 = I.initial_state(n, perturb=1e-3, seed=1)
