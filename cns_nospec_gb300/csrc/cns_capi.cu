@@ -475,6 +475,8 @@ struct WorkLists {
     int nx32 = 0;
     const Tile* w32 = nullptr;  // mixed boxes on the warp-specialised TMA assembly
     int nw32 = 0;
+    const Tile* dx32 = nullptr;  // the derivative pass of mixed boxes on either TMA assembly
+    int ndx32 = 0;
 };
 
 // One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
@@ -498,6 +500,10 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
         }
         if (w.nd32) {
             CK(launch_deriv(1, views, w.d32, w.nd32, stage, st));
+            if ((rc = mark(CNS_KERN_DERIV))) return rc;
+        }
+        if (w.ndx32) {
+            CK(launch_deriv_tma(views, w.dx32, w.ndx32, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
         if (w.nd64) {
@@ -524,13 +530,12 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
 static WorkLists box_lists(const cns_box* b) {
     WorkLists w;
     if (b->desc.precision == CNS_MIXED) {
-        w.d32 = b->d_tiles, w.nd32 = b->ntiles;
         if (b->kernel == CNS_ASSEMBLE_TMA)
-            w.x32 = b->d_xtiles, w.nx32 = b->nxtiles;
+            w.dx32 = w.x32 = b->d_xtiles, w.ndx32 = w.nx32 = b->nxtiles;
         else if (b->kernel == CNS_ASSEMBLE_TMA_WS)
-            w.w32 = b->d_xtiles, w.nw32 = b->nxtiles;
+            w.dx32 = w.w32 = b->d_xtiles, w.ndx32 = w.nw32 = b->nxtiles;
         else
-            w.a32 = b->d_tiles, w.na32 = b->ntiles;
+            w.d32 = w.a32 = b->d_tiles, w.nd32 = w.na32 = b->ntiles;
     } else {
         w.d64 = b->d_tiles, w.nd64 = b->ntiles;
     }
@@ -736,7 +741,7 @@ extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->member
 static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
-    std::vector<Tile> d64, d32, a32, x32, w32;  // the five lists of WorkLists
+    std::vector<Tile> d64, d32, a32, x32, w32, dx32;  // the lists of WorkLists
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
@@ -744,17 +749,17 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
             append_tiles(b->desc.n, b->view.tlog, (int)m, d64);
             continue;
         }
-        append_tiles(b->desc.n, b->view.tlog, (int)m, d32);
-        if (b->kernel == CNS_ASSEMBLE_TMA)
-            append_xtiles(b->desc.n, (int)m, x32);
-        else if (b->kernel == CNS_ASSEMBLE_TMA_WS)
-            append_xtiles(b->desc.n, (int)m, w32);
-        else
+        if (b->kernel == CNS_ASSEMBLE_TMA || b->kernel == CNS_ASSEMBLE_TMA_WS) {
+            append_xtiles(b->desc.n, (int)m, dx32);
+            append_xtiles(b->desc.n, (int)m, b->kernel == CNS_ASSEMBLE_TMA ? x32 : w32);
+        } else {
+            append_tiles(b->desc.n, b->view.tlog, (int)m, d32);
             append_tiles(b->desc.n, b->view.tlog, (int)m, a32);
+        }
     }
     std::vector<Tile> all;
-    all.reserve(d64.size() + d32.size() + a32.size() + x32.size() + w32.size());
-    for (auto* v : {&d64, &d32, &a32, &x32, &w32}) all.insert(all.end(), v->begin(), v->end());
+    all.reserve(d64.size() + d32.size() + a32.size() + x32.size() + w32.size() + dx32.size());
+    for (auto* v : {&d64, &d32, &a32, &x32, &w32, &dx32}) all.insert(all.end(), v->begin(), v->end());
     const size_t nt = all.size();
     if (views.size() > bt->cap_views) {
         cudaFree(bt->d_views);
@@ -777,7 +782,8 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     w.d32 = at, w.nd32 = (int)d32.size(), at += d32.size();
     w.a32 = at, w.na32 = (int)a32.size(), at += a32.size();
     w.x32 = at, w.nx32 = (int)x32.size(), at += x32.size();
-    w.w32 = at, w.nw32 = (int)w32.size();
+    w.w32 = at, w.nw32 = (int)w32.size(), at += w32.size();
+    w.dx32 = at, w.ndx32 = (int)dx32.size();
     bt->nviews = (int)views.size();
     if (bt->gexec) {
         cudaGraphExecDestroy(bt->gexec);

@@ -92,13 +92,12 @@ __device__ __forceinline__ void tma_load(float* dst, const CUtensorMap* map, int
         : "memory");
 }
 
-// Issue load number g of this block (tile g / 20, entry g % 20) into buffer g & 1.
-__device__ __forceinline__ void issue(const BoxView* boxes, const Tile* tiles, int tile, int entry, int flip,
-                                      float* buf, uint64_t* bar) {
+// Issue the copy of `L` for tile `tile` into `buf`, completing on `bar`.
+__device__ __forceinline__ void issue_load(const BoxView* boxes, const Tile* tiles, int tile, const Load L, int flip,
+                                           float* buf, uint64_t* bar) {
     const Tile T = tiles[tile];
     const BoxView& b = boxes[T.box];
     const TmaMaps* maps = (const TmaMaps*)b.tma;
-    const Load L = kSched[entry];
     const CUtensorMap* map;
     if (L.set == 0) {
         map = &maps->p[b.sc->pbase ^ flip][L.shape];  // stage s reads P[pbase ^ ((s-1)&1)]
@@ -109,6 +108,11 @@ __device__ __forceinline__ void issue(const BoxView* boxes, const Tile* tiles, i
     const int hk = box_k(L.shape) == XK ? 0 : 4, hj = box_j(L.shape) == XJ ? 0 : 4, hi = box_i(L.shape) == XI ? 0 : 4;
     mbar_expect_tx(bar, (uint32_t)(box_elems(L.shape) * sizeof(float)));
     tma_load(buf, map, T.k0 + CNS_NG - hk, T.j0 + CNS_NG - hj, T.i0 + CNS_NG - hi, L.field, bar);
+}
+// Load number g of this block in kSched (tile g / 20, entry g % 20).
+__device__ __forceinline__ void issue(const BoxView* boxes, const Tile* tiles, int tile, int entry, int flip,
+                                      float* buf, uint64_t* bar) {
+    issue_load(boxes, tiles, tile, kSched[entry], flip, buf, bar);
 }
 
 // ---- per-field consumers (compile-time box extents) ----------------------------------------
@@ -663,6 +667,92 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
     }
 }
 
+// ---- the mixed form's derivative pass, TMA-staged -------------------------------------------
+// Same tiles as the assembly; u, v, w of the stage's P set arrive as full-halo boxes,
+// double-buffered; the nine first derivatives come from shared memory with the operations of
+// k_deriv (cns_fused.cu) in the same order, and the S fields are stored as k_deriv stores them,
+// so the two give the same bits.  Waits bounded as in k_assemble_tma.
+__global__ void __launch_bounds__(kTileThreads, 2) k_deriv_tma(const BoxView* __restrict__ boxes,
+                                                            const Tile* __restrict__ tiles, int ntiles, int stage) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* buf[2] = {(float*)smem_raw, (float*)smem_raw + kBufElems};
+    uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(float));
+    const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
+    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    if (my_tiles <= 0) return;
+    const int total = my_tiles * 3;
+    if (tid == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int flip = (stage - 1) & 1;
+    auto load_of = [](int e) { return Load{0, (unsigned char)(PU + e), BX_FULL}; };  // u, v, w
+    if (tid == 0) issue_load(boxes, tiles, blockIdx.x, load_of(0), flip, buf[0], &bar[0]);
+    float d[3][3][XI];  // d[field][axis][cell]: u_x u_y u_z, v_x ..., w_x ...
+    int g = 0;
+    for (int it = 0; it < my_tiles; it++) {
+        const Tile T = tiles[blockIdx.x + it * gridDim.x];
+        const BoxView& b = boxes[T.box];
+        const CoefT<float>& cf = b.c32;
+#pragma unroll
+        for (int e = 0; e < 3; e++, g++) {
+            if (tid == 0 && g + 1 < total)
+                issue_load(boxes, tiles, blockIdx.x + ((g + 1) / 3) * gridDim.x, load_of((g + 1) % 3), flip,
+                           buf[(g + 1) & 1], &bar[(g + 1) & 1]);
+            const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                    mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+                    if (g + 1 < total) mbar_wait_bounded(&bar[(g + 1) & 1], (uint32_t)(((g + 1) >> 1) & 1));
+                }
+                return;
+            }
+            using B = Bx<BX_FULL>;
+            const float* s = buf[g & 1];
+            float col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk + 4)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                const float* p = s + B::at(i + 4, tj + 4, tk + 4);
+                d[e][0][i] = cd1(col, i + 4, cf.da[0]);
+                d[e][1][i] = sd1(p, B::K, cf.da[1]);
+                d[e][2][i] = sd1(p, 1, cf.da[2]);
+            }
+            __syncthreads();  // buffer g & 1 is free for load g + 2
+        }
+        // cpu/diffterm.cpp:294-304, as in k_deriv
+        const int j = T.j0 + tj, k = T.k0 + tk;
+        float* S = (float*)b.S;
+        const long long fs = b.fs;
+#pragma unroll
+        for (int i = 0; i < XI; i++) {
+            const int ic = T.i0 + i;
+            if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+            const float ux = d[0][0][i], uy = d[0][1][i], uz = d[0][2][i];
+            const float vx = d[1][0][i], vy = d[1][1][i], vz = d[1][2][i];
+            const float wx = d[2][0][i], wy = d[2][1][i], wz = d[2][2][i];
+            const float divu = (float)(2.0 / 3.0) * (ux + vy + wz);
+            const float tauxx = fmaf(2.0f, ux, -divu), tauyy = fmaf(2.0f, vy, -divu), tauzz = fmaf(2.0f, wz, -divu);
+            const float tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
+            float phi = tauxx * ux;
+            phi = fmaf(tauyy, vy, phi);
+            phi = fmaf(tauzz, wz, phi);
+            phi = fmaf(tauxy, tauxy, phi);
+            phi = fmaf(tauxz, tauxz, phi);
+            phi = fmaf(tauyz, tauyz, phi);
+            const long long c = cell_off(b, ic, j, k);
+            store_img(S + SX * fs, b, c, ic, j, k, vy + wz, 1);
+            store_img(S + SY * fs, b, c, ic, j, k, ux + wz, 2);
+            store_img(S + SZ * fs, b, c, ic, j, k, ux + vy, 4);
+            S[SPHI * fs + c] = cf.eta * phi;
+        }
+    }
+}
+
 // Self-test of the bounded wait: an mbarrier nothing ever arrives on.  The wait must give up
 // after its limit and the block must report HEALTH_TIMEOUT and return normally.
 __global__ void k_bounded_wait_selftest(int* out) {
@@ -761,6 +851,29 @@ cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int nti
     if (stage == 1) return launch_tma_stage<1>(boxes, tiles, ntiles, st);
     if (stage == 2) return launch_tma_stage<2>(boxes, tiles, ntiles, st);
     return launch_tma_stage<3>(boxes, tiles, ntiles, st);
+}
+
+template <class Fn>
+static cudaError_t launch_tma_grid(Fn fn, int nthreads, size_t smem, int ntiles, int* grid) {
+    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, nthreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    *grid = ntiles < nsm * per ? ntiles : nsm * per;
+    return cudaSuccess;
+}
+
+cudaError_t launch_deriv_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    int grid = 0;
+    cudaError_t e = launch_tma_grid(k_deriv_tma, kTileThreads, kTmaSmem, ntiles, &grid);
+    if (e != cudaSuccess) return e;
+    k_deriv_tma<<<grid, kTileThreads, kTmaSmem, st>>>(boxes, tiles, ntiles, stage);
+    return cudaGetLastError();
 }
 
 constexpr size_t kWsSmem = (kWsBufs * kBufElems + 2 * kStashElems) * sizeof(float) + (kWsBufs + 4) * sizeof(uint64_t);
