@@ -183,9 +183,23 @@ def cpu_baseline(n: int, seconds: float):
         el = time.perf_counter() - t0
         if el >= seconds or steps >= 100:
             break
+    # one core, as the reference's own cpu/ path runs (its OpenMP pragmas are commented out)
+    one = {}
+    O.set_threads(1)
+    for m, budget in ((32, 1.0), (n, 3.0)):
+        V = I.initial_state(m, perturb=1e-3, seed=1)
+        k, t1 = 0, time.perf_counter()
+        while True:
+            V, _ = O.advance(V, 1, I.box_dx(m), I.CFL, I.ETA, I.ALAM, which="port")
+            k += 1
+            e1 = time.perf_counter() - t1
+            if e1 >= budget or k >= 50:
+                break
+        one[str(m)] = m ** 3 * k / e1
+    O.set_threads(threads)
     return {"value": n ** 3 * steps / el, "unit": "cell-updates/s", "cores": threads, "kind": "port",
             "sample": f"{steps} RK3 step(s) of the {n}^3 box, {threads} OpenMP threads, {el:.1f} s",
-            "reference_lib_present": which == "ref"}
+            "one_core_by_n": one, "reference_lib_present": which == "ref"}
 
 
 def run_reference(args, dist):
