@@ -62,6 +62,8 @@ SIGNATURES = {
     "cns_new_advance": (C.c_int, [C.POINTER(GlobalConst), _D, _D, _D, _D, _D, _D]),
     "cns_host_in_place": (C.c_int, [_VP, C.c_longlong, _I]),
     "cns_advance_host": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _D]),
+    "cns_advance_f64": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, _D]),
+    "cns_advance_mixed": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, _D]),
     "cns_box_bytes": (C.c_longlong, [C.POINTER(BoxDesc)]),
     "cns_box_create": (C.c_int, [C.POINTER(BoxDesc), C.POINTER(_VP)]),
     "cns_box_destroy": (C.c_int, [_VP]),

@@ -1098,6 +1098,15 @@ extern "C" int cns_advance_host(double* U, const int n[3], const double dx[3], d
     return host_advance(d, U, nsteps, dt_hist);
 }
 
+extern "C" int cns_advance_f64(double* U, const int n[3], const double dx[3], double cfl, double eta, double alam,
+                               int nsteps, double* dt_hist) {
+    return cns_advance_host(U, n, dx, cfl, eta, alam, nsteps, CNS_FP64, dt_hist);
+}
+extern "C" int cns_advance_mixed(double* U, const int n[3], const double dx[3], double cfl, double eta, double alam,
+                                 int nsteps, double* dt_hist) {
+    return cns_advance_host(U, n, dx, cfl, eta, alam, nsteps, CNS_MIXED, dt_hist);
+}
+
 extern "C" int cns_host_in_place(const void* U, long long bytes, int* in_place) {
     if (!U || !in_place || bytes < 0) return fail(CNS_ERR_INVALID, "null argument or negative size");
     *in_place = mapped_host_range(U, (size_t)bytes) ? 1 : 0;

@@ -130,6 +130,11 @@ int cns_new_advance(const cns_global_const_t *h, double *U, double *Unew, double
  * dt_hist (nullable) receives each step's dt.  precision: cns_precision. */
 int cns_advance_host(double *U, const int n[3], const double dx[3], double cfl, double eta, double alam,
                      int nsteps, int precision, double *dt_hist);
+/* cns_advance_host with precision CNS_FP64 / CNS_MIXED. */
+int cns_advance_f64(double *U, const int n[3], const double dx[3], double cfl, double eta, double alam, int nsteps,
+                    double *dt_hist);
+int cns_advance_mixed(double *U, const int n[3], const double dx[3], double cfl, double eta, double alam, int nsteps,
+                      double *dt_hist);
 
 /* Host arrays: when all of [U, U + bytes) lies in one page-locked allocation the device can
  * address (cudaHostAlloc, cudaHostRegister, a pinned torch tensor), cns_new_advance,

@@ -92,3 +92,18 @@ def test_box_upload_download_pinned_equals_pageable(gpu, cns, precision):
         outs.append(dst.copy())
         box.close()
     assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_named_entry_points_equal_advance_host(gpu, cns, precision):
+    """cns_advance_f64 / cns_advance_mixed are cns_advance_host with the precision fixed."""
+    from cns_nospec_gb300 import _lib as L
+    from cns_nospec_gb300 import initdata as I
+    n = (12, 16, 20)
+    U0 = I.initial_state(n, perturb=1e-3, seed=11)
+    a, b = U0.copy(), U0.copy()
+    cns.advance_host(a, 2, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision)
+    fn = gpu.cns_advance_f64 if precision == 0 else gpu.cns_advance_mixed
+    dts = np.zeros(2)
+    L.check(fn(L.dptr(b), L.iarr(list(n)), L.darr(I.box_dx(n)), I.CFL, I.ETA, I.ALAM, 2, L.dptr(dts)))
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
