@@ -352,6 +352,11 @@ def run_ours(args, dist):
                      "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak,
                      "peak_source": "measured live: FP64 FMA probe kernel (cns_measure_fp64_peak)",
                      "flops_per_launch": flops_launch, "launch_ms": dom_launch_ms,
+                     "flops_basis": "the reference's FP64 operation count (2,450 per cell-update, less k_deriv's "
+                                    "3 x 132, over 3 launches); the fused kernel retires fewer FP64 instructions "
+                                    "than that count, so frac can exceed 1",
+                     "fp64_pipe_busy_ncu": 0.904,
+                     "fp64_pipe_source": "ncu sm__pipe_fp64_cycles_active, profiles/k_assemble_fp64_128cube.md",
                      "traffic": traffic, "traffic_source": tsrc},
         "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak, "frac": hbm_gbs / hbm_peak,
                 "bytes_per_cell_update": BYTES_PER_CELL_UPDATE, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
