@@ -111,11 +111,15 @@ static int validate_desc(const cns_box_desc* d) {
 // ---- tile shapes ----------------------------------------------------------------------------
 // Candidate tile shapes (log2 of the i, j, k extents; 256 cells each).  k is the unit-stride
 // axis, so every candidate keeps at least 8 consecutive k cells in a warp.
+// The last candidate is the linear tile (256 consecutive cells; cns_common.cuh).
 static const int kShapes[][3] = {{1, 2, 5}, {0, 3, 5}, {2, 1, 5}, {0, 2, 6}, {1, 1, 6},
-                                 {1, 3, 4}, {2, 2, 4}, {0, 4, 4}, {3, 1, 4}, {2, 3, 3}, {3, 2, 3}, {1, 4, 3}};
+                                 {1, 3, 4}, {2, 2, 4}, {0, 4, 4}, {3, 1, 4}, {2, 3, 3}, {3, 2, 3}, {1, 4, 3},
+                                 {kLinearTile, 0, 0}};
 static const int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+static const int kNumBlockShapes = kNumShapes - 1;  // the rectangular ones
 
 static long long tile_count(const int n[3], const int tlog[3]) {
+    if (tlog[0] == kLinearTile) return ((long long)n[0] * n[1] * n[2] + kTileThreads - 1) / kTileThreads;
     long long c = 1;
     for (int a = 0; a < 3; a++) c *= (n[a] + (1 << tlog[a]) - 1) >> tlog[a];
     return c;
@@ -124,7 +128,7 @@ static long long tile_count(const int n[3], const int tlog[3]) {
 // The candidate that pads the box least (ties: the earlier candidate in the list).
 static void default_tlog(const int n[3], int out[3]) {
     long long best = -1;
-    for (int s = 0; s < kNumShapes; s++) {
+    for (int s = 0; s < kNumBlockShapes; s++) {
         const long long cells = tile_count(n, kShapes[s]) * kTileThreads;
         if (best < 0 || cells < best) {
             best = cells;
@@ -134,6 +138,11 @@ static void default_tlog(const int n[3], int out[3]) {
 }
 
 static void append_tiles(const int n[3], const int tlog[3], int box_index, std::vector<Tile>& out) {
+    if (tlog[0] == kLinearTile) {
+        const long long nt = tile_count(n, tlog);
+        for (long long t = 0; t < nt; t++) out.push_back(Tile{box_index, 0, 0, (int)t});
+        return;
+    }
     const int ti = 1 << tlog[0], tj = 1 << tlog[1], tk = 1 << tlog[2];
     for (int i0 = 0; i0 < n[0]; i0 += ti)
         for (int j0 = 0; j0 < n[1]; j0 += tj)
@@ -1210,6 +1219,7 @@ extern "C" int cns_box_load(cns_box* b, const char* path) {
 
 // ---- tile shapes and the autotuner ---------------------------------------------------------
 static int valid_tlog(const int t[3]) {
+    if (t[0] == kLinearTile) return t[1] == 0 && t[2] == 0;
     for (int a = 0; a < 3; a++)
         if (t[a] < 0 || t[a] > 8) return 0;
     return t[0] + t[1] + t[2] == 8 && t[2] >= 3;
@@ -1224,7 +1234,8 @@ extern "C" int cns_box_get_tile(const cns_box* b, int tlog[3]) {
 // Apply a tile shape to a box's own work list and device view (the batch, if any, is rebuilt
 // lazily).  Results do not depend on the shape: every cell's arithmetic is the same.
 static int apply_tile(cns_box* b, const int tlog[3]) {
-    if (!valid_tlog(tlog)) return fail(CNS_ERR_INVALID, "tile shape: log2 extents in [0,8] summing to 8, k >= 3");
+    if (!valid_tlog(tlog))
+        return fail(CNS_ERR_INVALID, "tile shape: log2 extents in [0,8] summing to 8, k >= 3, or {-1, 0, 0} (linear)");
     if (tile_count(b->desc.n, tlog) > b->geo.ntiles) return fail(CNS_ERR_CAPACITY, "tile shape has too many tiles");
     CK(cudaStreamSynchronize(b->stream));
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));

@@ -121,6 +121,28 @@ __device__ __forceinline__ void tile_cell(const int tlog[3], int t, int* ti, int
     *ti = t >> (lk + lj);
 }
 
+// A box whose tlog[0] is kLinearTile uses linear tiles: tile T is the 256 consecutive cells
+// 256 * T.k0 ... of the box's interior in its own order (i slowest, k fastest), so no box shape
+// pads a tile; a warp still covers 32 consecutive k cells except where a k row ends.
+constexpr int kLinearTile = -1;
+
+// The cell of thread t of tile T (i >= n[0] past the end of a box: the caller skips it).
+__device__ __forceinline__ void tile_pos(const BoxView& b, const Tile& T, int t, int* i, int* j, int* k) {
+    if (b.tlog[0] == kLinearTile) {
+        const long long p = (long long)T.k0 * kTileThreads + t;
+        const long long row = p / b.n[2];
+        *k = (int)(p - row * b.n[2]);
+        *j = (int)(row % b.n[1]);
+        *i = (int)(row / b.n[1]);
+    } else {
+        int ti, tj, tk;
+        tile_cell(b.tlog, t, &ti, &tj, &tk);
+        *i = T.i0 + ti;
+        *j = T.j0 + tj;
+        *k = T.k0 + tk;
+    }
+}
+
 __host__ __device__ inline long long cell_off(const BoxView& b, int i, int j, int k) {
     // (i, j, k) interior indices, 0-based; returns the element offset inside one field
     return (long long)(i + CNS_NG) * b.si + (long long)(j + CNS_NG) * b.sj + (k + CNS_NG);

@@ -18,9 +18,8 @@ __global__ void __launch_bounds__(kTileThreads) k_prim(const BoxView* __restrict
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
-        int ti, tj, tk;
-        tile_cell(b.tlog, threadIdx.x, &ti, &tj, &tk);
-        const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
+        int i, j, k;
+        tile_pos(b, T, threadIdx.x, &i, &j, &k);
         double cour = 0.0;
         int health = 0;
         if (i < b.n[0] && j < b.n[1] && k < b.n[2]) {
@@ -43,9 +42,8 @@ __global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restric
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
-        int ti, tj, tk;
-        tile_cell(b.tlog, threadIdx.x, &ti, &tj, &tk);
-        const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
+        int i, j, k;
+        tile_pos(b, T, threadIdx.x, &i, &j, &k);
         if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
         const int pr = b.sc->pbase ^ ((stage - 1) & 1);
         const R* P = (const R*)b.P[pr];
@@ -83,9 +81,8 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
-        int ti, tj, tk;
-        tile_cell(b.tlog, threadIdx.x, &ti, &tj, &tk);
-        const int i = T.i0 + ti, j = T.j0 + tj, k = T.k0 + tk;
+        int i, j, k;
+        tile_pos(b, T, threadIdx.x, &i, &j, &k);
         double cour = 0.0;
         int health = 0;
         if (i < b.n[0] && j < b.n[1] && k < b.n[2]) {

@@ -220,7 +220,9 @@ int cns_batch_sync(cns_batch *batch);
 
 /* ---- tile shapes and the autotuner -------------------------------------------------------
  * Work is cut into tiles of 256 cells (one per thread, k fastest across a warp); a box's tile
- * shape is tlog[3] = log2 of the tile's (i, j, k) extents, summing to 8 with tlog[2] >= 3.
+ * shape is tlog[3] = log2 of the tile's (i, j, k) extents, summing to 8 with tlog[2] >= 3, or
+ * {-1, 0, 0}: linear tiles of 256 consecutive cells in the box's own order (no padding for any
+ * box shape).
  * The shape changes only speed, never results: every cell's arithmetic is the same.
  * A new box starts on the candidate shape that pads it least. */
 int cns_box_get_tile(const cns_box *box, int tlog[3]);
@@ -234,13 +236,13 @@ int cns_box_set_tile(cns_box *box, const int tlog[3]);
 enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2 };
 int cns_box_get_kernel(const cns_box *box, int *kernel);
 int cns_box_set_kernel(cns_box *box, int kernel);
-/* Time trial_steps RK3 steps of the box on every candidate shape (and, for mixed boxes, both
- * assembly kernels) and keep the fastest; the box's state is restored afterwards, so the run
+/* Time trial_steps RK3 steps of the box on every candidate shape (the 12 rectangular ones and
+ * the linear one; for mixed boxes, with each of the three assembly kernels) and keep the fastest; the box's state is restored afterwards, so the run
  * continues bit for bit.  Blocks. */
 int cns_box_autotune(cns_box *box, int trial_steps, int tlog_out[3], int *kernel_out, double *best_ms_per_step);
-/* Same for a batch.  Policy p = shape + 13 * kernel: shape 0 = every member on its
- * least-padding shape, 1 + s = every member on candidate shape s; kernel = the assembly kernel
- * of its mixed members.  The fastest policy is kept and the graph re-captured. */
+/* Same for a batch.  Policy p = shape + 14 * kernel: shape 0 = every member on its
+ * least-padding rectangular shape, 1 + s = every member on candidate shape s (s = 12: linear);
+ * kernel = the assembly kernel of its mixed members.  The fastest policy is kept and the graph re-captured. */
 int cns_batch_autotune(cns_batch *batch, int trial_steps, int *chosen_policy, double *best_ms_per_step);
 
 #ifdef __cplusplus
