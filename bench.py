@@ -49,8 +49,9 @@ def parse():
     p.add_argument("--size", dest="n", type=int, default=128, help="cells per axis of the periodic box")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
-    p.add_argument("--case", choices=["fp64", "mixed"], default=None,
-                   help="profiling case: only upload + warmup + steps of one form (for ncu), then exit")
+    p.add_argument("--case", choices=["fp64", "mixed", "e2e"], default=None,
+                   help="profiling case: only upload + warmup + steps of one form (for ncu), then exit; "
+                        "e2e: warmup + steps calls of cns_new_advance on a page-locked host array")
     p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve"], default="box",
                    help="box: the headline 128^3 line (default); batch: 256 uneven boxes; "
                         "mixed256: FP64 vs mixed at --size (use 256); serve: the request stream")
@@ -393,6 +394,20 @@ def run_case(args):
     from cns_nospec_gb300 import initdata as I
     lib = C.load()
     L.check(lib.cns_set_device(0))
+    if args.case == "e2e":
+        Uh, pinned, _keep = pinned_like((args.n + 8,) * 3 + (5,))
+        Uh[...] = I.initial_state(args.n, perturb=1e-3, seed=1)
+        h = C.read_configurations(args.n, I.box_dx(args.n), I.CFL, I.ETA, I.ALAM)
+        for _ in range(args.warmup):
+            C.new_advance(Uh, None, None, None, None, h)
+        lib.cns_device_synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            C.new_advance(Uh, None, None, None, None, h)
+        lib.cns_device_synchronize()
+        print(json.dumps({"case": "e2e", "n": args.n, "calls": args.steps, "pinned_host": pinned,
+                          "ms_per_call": 1e3 * (time.perf_counter() - t0) / max(args.steps, 1)}))
+        return
     prec = C.CNS_FP64 if args.case == "fp64" else C.CNS_MIXED
     box = C.Box(args.n, I.box_dx(args.n), I.CFL, I.ETA, I.ALAM, precision=prec)
     box.init_field(perturb=1e-3, seed=1)
