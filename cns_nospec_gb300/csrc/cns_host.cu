@@ -195,16 +195,14 @@ cudaError_t host_ghosts(const BoxView& v, double* h, cudaStream_t st) {
 typedef CUresult (*PointerGetAttributeFn)(void*, CUpointer_attribute, CUdeviceptr);
 
 static PointerGetAttributeFn pointer_attr_fn() {
-    static PointerGetAttributeFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const PointerGetAttributeFn fn = [] {  // looked up once, thread-safely
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PointerGetAttributeFn)p;
-    }
+            return (PointerGetAttributeFn)p;
+        return (PointerGetAttributeFn) nullptr;
+    }();
     return fn;
 }
 
