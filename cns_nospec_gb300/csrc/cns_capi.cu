@@ -252,6 +252,10 @@ struct cns_box {
     cudaGraphExec_t gexec = nullptr;
     cns_batch* batch = nullptr;
     double* host_out = nullptr;  // the source of the device view's host_out (see set_host_out)
+    int* d_queue = nullptr;      // k_upload_deriv's work queue for the tile shape queue_tlog
+    int nq = 0;
+    int queue_tlog[3] = {0, 0, 0};
+    int* d_counters = nullptr;   // its plane counts and queue position (n[0] + 1 ints)
 };
 
 extern "C" long long cns_box_bytes(const cns_box_desc* desc) {
@@ -357,6 +361,11 @@ extern "C" int cns_box_destroy(cns_box* b) {
         cns_batch_remove(b->batch, b);
     }
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->d_queue || b->d_counters) {
+        cudaStreamSynchronize(b->stream);
+        cudaFree(b->d_queue);
+        cudaFree(b->d_counters);
+    }
     cudaFreeAsync(b->arena, b->stream);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);  // released once its queued work is done
     delete b;
@@ -490,8 +499,10 @@ struct WorkLists {
 
 // One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
 // every launch and the launch's kind appended to `kinds`.
+// With skip_first_deriv the step starts at stage 1's assembly (its derivative pass already ran,
+// fused with an upload).
 static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cudaStream_t st,
-                        std::vector<cudaEvent_t>* ev, std::vector<int>* kinds) {
+                        std::vector<cudaEvent_t>* ev, std::vector<int>* kinds, bool skip_first_deriv = false) {
     auto mark = [&](int kind) -> int {
         if (!ev) return CNS_OK;
         cudaEvent_t e;
@@ -503,15 +514,15 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
     };
     int rc;
     for (int stage = 1; stage <= 3; stage++) {
-        if (w.nd64) {
+        if (w.nd64 && !(stage == 1 && skip_first_deriv)) {
             CK(launch_deriv(0, views, w.d64, w.nd64, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
-        if (w.nd32) {
+        if (w.nd32 && !(stage == 1 && skip_first_deriv)) {
             CK(launch_deriv(1, views, w.d32, w.nd32, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
-        if (w.ndx32) {
+        if (w.ndx32 && !(stage == 1 && skip_first_deriv)) {
             CK(launch_deriv_tma(views, w.dx32, w.ndx32, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
@@ -1043,6 +1054,32 @@ struct HostOutGuard {
     }
 };
 
+// FP64 box, page-locked host array: upload it and enqueue the first RK3 step, with stage 1's
+// derivative pass fused into the upload (k_upload_deriv, cns_host.cu): the FP64-bound
+// derivatives run while the link-bound upload is still reading.  Same arithmetic, same bits as
+// upload + step.
+static int upload_first_step(cns_box* b, double* h_map, bool ghosts) {
+    if (!b->d_queue || memcmp(b->queue_tlog, b->view.tlog, sizeof b->queue_tlog) != 0) {
+        std::vector<Tile> tiles;
+        append_tiles(b->desc.n, b->view.tlog, 0, tiles);
+        const std::vector<int> q = upload_deriv_queue(b->desc.n, b->view.tlog, tiles);
+        CK(cudaStreamSynchronize(b->stream));
+        cudaFree(b->d_queue);
+        b->d_queue = nullptr;
+        CK(cudaMalloc((void**)&b->d_queue, sizeof(int) * q.size()));
+        CK(cudaMemcpy(b->d_queue, q.data(), sizeof(int) * q.size(), cudaMemcpyHostToDevice));
+        b->nq = (int)q.size();
+        memcpy(b->queue_tlog, b->view.tlog, sizeof b->queue_tlog);
+    }
+    if (!b->d_counters) CK(cudaMalloc((void**)&b->d_counters, sizeof(int) * (b->desc.n[0] + 1)));
+    CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
+    CK(host_upload_deriv(b->view, h_map, ghosts, b->d_tiles, b->d_queue, b->nq, b->d_counters, b->stream));
+    CK(launch_refs(b->d_view, 1, b->stream));
+    CK(launch_stepend(b->d_view, 1, 0, b->stream));
+    b->primed = true;
+    return enqueue_step(b->d_view, 1, box_lists(b), b->stream, nullptr, nullptr, true);
+}
+
 static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt_hist) {
     cns_box* b;
     int rc = cached_box(d, &b);
@@ -1052,12 +1089,21 @@ static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt
     guard.b = b;
     // the last step's start state supplies the ghosts: with at most one step that is the input
     const bool ghosts_on_upload = h_map && nsteps <= 1;
-    if ((rc = upload_host(b, U, h_map, ghosts_on_upload))) return rc;
+    // FP64 boxes on page-locked memory: the first step's derivative pass rides with the upload
+    const bool fused = h_map && b->desc.precision == CNS_FP64 && nsteps >= 1;
+    if (fused) {
+        if (nsteps == 1 && (rc = set_host_out(b, h_map))) return rc;  // the first step is the last
+        if ((rc = upload_first_step(b, h_map, ghosts_on_upload))) return rc;
+        if (nsteps == 1 && (rc = set_host_out(b, nullptr))) return rc;
+    } else if ((rc = upload_host(b, U, h_map, ghosts_on_upload))) {
+        return rc;
+    }
     int done = 0;
     while (done < nsteps) {
         const int chunk = std::min(nsteps - done, DTLOG_CAP);
-        if (done + chunk == nsteps) {
-            if (chunk > 1 && (rc = cns_box_advance(b, chunk - 1))) return rc;
+        const int first = (done == 0 && fused) ? 1 : 0;  // steps of this chunk already enqueued
+        if (done + chunk == nsteps && chunk > first) {
+            if (chunk - 1 > first && (rc = cns_box_advance(b, chunk - 1 - first))) return rc;
             if (!h_map)
                 CK(op_box_to_aos(b->view, b->d_aos, 1, b->stream));
             else if (!ghosts_on_upload)
@@ -1066,7 +1112,7 @@ static int host_advance(const cns_box_desc& d, double* U, int nsteps, double* dt
             if (h_map && (rc = set_host_out(b, h_map))) return rc;
             if ((rc = cns_box_advance(b, 1))) return rc;
             if (h_map && (rc = set_host_out(b, nullptr))) return rc;
-        } else if ((rc = cns_box_advance(b, chunk))) {
+        } else if (chunk > first && (rc = cns_box_advance(b, chunk - first))) {
             return rc;
         }
         if (dt_hist) {

@@ -45,32 +45,7 @@ __global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restric
         int i, j, k;
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
         if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
-        const int pr = b.sc->pbase ^ ((stage - 1) & 1);
-        const R* P = (const R*)b.P[pr];
-        R* S = (R*)b.S;
-        const long long c = cell_off(b, i, j, k), fs = b.fs, si = b.si, sj = b.sj;
-        const CoefT<R>& cf = coefs<R>(b);
-        const R* pu = P + PU * fs + c;
-        const R* pv = P + PV * fs + c;
-        const R* pw = P + PW * fs + c;
-        // cpu/diffterm.cpp:73-151 (the nine first derivatives), at this cell only
-        const R ux = d1(pu, si, cf.da[0]), uy = d1(pu, sj, cf.da[1]), uz = d1(pu, 1, cf.da[2]);
-        const R vx = d1(pv, si, cf.da[0]), vy = d1(pv, sj, cf.da[1]), vz = d1(pv, 1, cf.da[2]);
-        const R wx = d1(pw, si, cf.da[0]), wy = d1(pw, sj, cf.da[1]), wz = d1(pw, 1, cf.da[2]);
-        // cpu/diffterm.cpp:294-304: viscous dissipation
-        const R divu = (R)(2.0 / 3.0) * (ux + vy + wz);
-        const R tauxx = fma((R)2, ux, -divu), tauyy = fma((R)2, vy, -divu), tauzz = fma((R)2, wz, -divu);
-        const R tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
-        R phi = tauxx * ux;
-        phi = fma(tauyy, vy, phi);
-        phi = fma(tauzz, wz, phi);
-        phi = fma(tauxy, tauxy, phi);
-        phi = fma(tauxz, tauxz, phi);
-        phi = fma(tauyz, tauyz, phi);
-        store_img(S + SX * fs, b, c, i, j, k, vy + wz, 1);
-        store_img(S + SY * fs, b, c, i, j, k, ux + wz, 2);
-        store_img(S + SZ * fs, b, c, i, j, k, ux + vy, 4);
-        S[SPHI * fs + c] = cf.eta * phi;
+        deriv_cell<R>(b, i, j, k, stage);
     }
 }
 

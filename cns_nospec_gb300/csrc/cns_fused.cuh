@@ -48,12 +48,20 @@ __device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, 
     acc = fma(a[3], __ldg(p + 4 * s) - __ldg(p - 4 * s), acc);
     return acc;
 }
-template <class R>
+// Loads of stencil taps: through the read-only path (NC, for data no thread of the launch
+// writes), or from L2 past L1 (for data other blocks of the same launch write: L1 is not kept
+// coherent, and a 128-byte line can hold bytes of a row that is not written yet).
+template <bool NC, class R>
+__device__ __forceinline__ R ld_tap(const R* p) {
+    if (NC) return __ldg(p);
+    return __ldcg(p);
+}
+template <class R, bool NC = true>
 __device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a) {
-    R acc = a[0] * (__ldg(p + s) - __ldg(p - s));
-    acc = fma(a[1], __ldg(p + 2 * s) - __ldg(p - 2 * s), acc);
-    acc = fma(a[2], __ldg(p + 3 * s) - __ldg(p - 3 * s), acc);
-    acc = fma(a[3], __ldg(p + 4 * s) - __ldg(p - 4 * s), acc);
+    R acc = a[0] * (ld_tap<NC>(p + s) - ld_tap<NC>(p - s));
+    acc = fma(a[1], ld_tap<NC>(p + 2 * s) - ld_tap<NC>(p - 2 * s), acc);
+    acc = fma(a[2], ld_tap<NC>(p + 3 * s) - ld_tap<NC>(p - 3 * s), acc);
+    acc = fma(a[3], ld_tap<NC>(p + 4 * s) - ld_tap<NC>(p - 4 * s), acc);
     return acc;
 }
 // acc + sum_m b_m (p[m s] + p[-m s])
@@ -93,6 +101,37 @@ __device__ __forceinline__ void store_host(const BoxView& b, int i, int j, int k
     double* h = b.host_out + (((long long)(i + CNS_NG) * g1 + (j + CNS_NG)) * g2 + (k + CNS_NG)) * CNS_NC;
 #pragma unroll
     for (int l = 0; l < CNS_NC; l++) h[l] = un[l];
+}
+
+// k_deriv's work at cell (i, j, k) of stage `stage`: the nine first derivatives of (u, v, w)
+// (cpu/diffterm.cpp:73-151) into the S sums and the viscous dissipation (cpu/diffterm.cpp:294-304).
+// NC = false reads the P set from L2 (ld_tap), for a launch whose other blocks write it.
+template <class R, bool NC = true>
+__device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k, int stage) {
+    const int pr = b.sc->pbase ^ ((stage - 1) & 1);
+    const R* P = (const R*)b.P[pr];
+    R* S = (R*)b.S;
+    const long long c = cell_off(b, i, j, k), fs = b.fs, si = b.si, sj = b.sj;
+    const CoefT<R>& cf = coefs<R>(b);
+    const R* pu = P + PU * fs + c;
+    const R* pv = P + PV * fs + c;
+    const R* pw = P + PW * fs + c;
+    const R ux = d1<R, NC>(pu, si, cf.da[0]), uy = d1<R, NC>(pu, sj, cf.da[1]), uz = d1<R, NC>(pu, 1, cf.da[2]);
+    const R vx = d1<R, NC>(pv, si, cf.da[0]), vy = d1<R, NC>(pv, sj, cf.da[1]), vz = d1<R, NC>(pv, 1, cf.da[2]);
+    const R wx = d1<R, NC>(pw, si, cf.da[0]), wy = d1<R, NC>(pw, sj, cf.da[1]), wz = d1<R, NC>(pw, 1, cf.da[2]);
+    const R divu = (R)(2.0 / 3.0) * (ux + vy + wz);
+    const R tauxx = fma((R)2, ux, -divu), tauyy = fma((R)2, vy, -divu), tauzz = fma((R)2, wz, -divu);
+    const R tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
+    R phi = tauxx * ux;
+    phi = fma(tauyy, vy, phi);
+    phi = fma(tauzz, wz, phi);
+    phi = fma(tauxy, tauxy, phi);
+    phi = fma(tauxz, tauxz, phi);
+    phi = fma(tauyz, tauyz, phi);
+    store_img(S + SX * fs, b, c, i, j, k, vy + wz, 1);
+    store_img(S + SY * fs, b, c, i, j, k, ux + wz, 2);
+    store_img(S + SZ * fs, b, c, i, j, k, ux + vy, 4);
+    S[SPHI * fs + c] = cf.eta * phi;
 }
 
 // Health bits from raw IEEE fields (integer ops only; no FP64 pipe work).

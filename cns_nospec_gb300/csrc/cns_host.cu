@@ -16,6 +16,10 @@
 // per-warp shared-memory buffer; the device side is the box's structure-of-arrays layout.
 #include <cuda.h>
 
+#include <algorithm>
+#include <climits>
+#include <vector>
+
 #include "cns_fused.cuh"
 #include "cns_internal.h"
 
@@ -157,6 +161,116 @@ __global__ void __launch_bounds__(kWarps * 32) k_host_ghosts(BoxView b, double* 
     }
 }
 
+// ---- the upload fused with stage 1's derivative pass (FP64 boxes) -------------------------
+// One persistent launch works through a queue built on the host (upload_deriv_queue): upload
+// items (8 runs of one i-plane, planes in the order n-4 .. n-1, 0 .. n-5) interleaved with the
+// derivative tiles of stage 1.  Each tile stands after the upload items of every plane it reads
+// (its own planes and 4 on each side, periodically) and kDerivLag more planes, so that by the
+// time a block takes it those planes are usually in.  Blocks take items in queue order from an
+// atomic counter.  A tile waits for its planes' completion counts; every upload item it waits
+// for stands earlier in the queue, so it was already taken by a running block that waits on
+// nothing: the waits always end.  They are bounded all the same (about one second of global
+// time; then HEALTH_TIMEOUT and the tile is skipped).  A warp publishes a finished run with a
+// fence before counting it; a tile fences after seeing its counts and reads the P set from L2
+// (deriv_cell<double, false>: it is written during this launch).
+constexpr int kPlaneStart = CNS_NG;  // plane order: q = (i + 4) mod n
+constexpr int kDerivLag = 8;         // planes (measured at 128^3: 4.68 ms per call, 4.85 unfused)
+
+__device__ __forceinline__ bool planes_ready(const volatile int* done, int n0, int lo, int hi, int target) {
+    for (int p = lo; p <= hi; p++)
+        if (done[(p % n0 + n0) % n0] < target) return false;
+    return true;
+}
+
+template <bool GHOSTS>
+__global__ void __launch_bounds__(kWarps * 32) k_upload_deriv(BoxView b, double* __restrict__ h,
+                                                               const Tile* __restrict__ tiles,
+                                                               const int* __restrict__ queue, int nq, int* counter,
+                                                               int* done) {
+    __shared__ double s[kWarps][kRun * CNS_NC];
+    __shared__ int s_item, s_ok;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double* sw = s[warp];
+    const int runs = (b.n[2] + kRun - 1) / kRun, per_plane = b.n[1] * runs;
+    const int items_per_plane = (per_plane + kWarps - 1) / kWarps;
+    const int g1 = b.n[1] + 2 * CNS_NG, g2 = b.n[2] + 2 * CNS_NG;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int pos = atomicAdd(counter, 1);
+            s_item = pos < nq ? queue[pos] : INT_MIN;
+        }
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();  // s_item is rewritten next round
+        if (item == INT_MIN) return;
+        if (item >= 0) {  // upload: run (item % items_per_plane) * 8 + warp of plane order q
+            const int q = item / items_per_plane, rr = (item % items_per_plane) * kWarps + warp;
+            if (rr >= per_plane) continue;  // warp-uniform; the next block barrier is at the loop top
+            RunIdx r;
+            r.i = (q + b.n[0] - kPlaneStart) % b.n[0];
+            r.j = rr / runs;
+            r.k0 = (rr % runs) * kRun;
+            r.cnt = min(kRun, b.n[2] - r.k0);
+            r.a0 = (((long long)(r.i + CNS_NG) * g1 + (r.j + CNS_NG)) * g2 + (r.k0 + CNS_NG)) * CNS_NC;
+            for (int x = lane; x < r.cnt * CNS_NC; x += 32) sw[x] = h[r.a0 + x];
+            __syncwarp();
+            if (GHOSTS) run_images(b, r, sw, h, lane);
+            double cour = 0.0;
+            int health = 0;
+            if (lane < r.cnt) {
+                const int k = r.k0 + lane;
+                const long long c = cell_off(b, r.i, r.j, k);
+                double un[CNS_NC];
+#pragma unroll
+                for (int l = 0; l < CNS_NC; l++) {
+                    un[l] = sw[lane * CNS_NC + l];
+                    b.U[c + l * b.fs] = un[l];
+                }
+                cour = epilogue<double>(b, (double*)b.P[b.sc->pbase], c, r.i, r.j, k, un, true, &health);
+            }
+            if (health) atomicOr(&b.sc->status, health);
+            courant_fold(b, cour);
+            __threadfence();  // this lane's stores, before the run is counted
+            __syncwarp();
+            if (lane == 0) atomicAdd(&done[r.i], 1);
+        } else {  // stage 1's derivative pass on tile ~item, once the planes it reads are in
+            const Tile T = tiles[~item];
+            int lo, hi;
+            if (b.tlog[0] == kLinearTile) {
+                const long long plane = (long long)b.n[1] * b.n[2], last = (long long)b.n[0] * plane - 1;
+                const long long p0 = (long long)T.k0 * kTileThreads;
+                lo = (int)(p0 / plane);
+                hi = (int)(min(p0 + kTileThreads - 1, last) / plane);
+            } else {
+                lo = T.i0;
+                hi = min(T.i0 + (1 << b.tlog[0]), b.n[0]) - 1;
+            }
+            lo -= CNS_NG;
+            hi += CNS_NG;
+            if (hi - lo >= b.n[0]) lo = 0, hi = b.n[0] - 1;
+            if (threadIdx.x == 0) {
+                bool ok = planes_ready(done, b.n[0], lo, hi, per_plane);
+                if (!ok) {
+                    unsigned long long t0, t;
+                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+                    do {
+                        ok = planes_ready(done, b.n[0], lo, hi, per_plane);
+                        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+                    } while (!ok && t - t0 < 1000000000ull);
+                }
+                if (!ok) atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                __threadfence();  // the counted runs' stores, before this tile's loads
+                s_ok = ok;
+            }
+            __syncthreads();
+            const bool ok = s_ok;
+            int i, j, k;
+            tile_pos(b, T, threadIdx.x, &i, &j, &k);
+            if (ok && i < b.n[0] && j < b.n[1] && k < b.n[2]) deriv_cell<double, false>(b, i, j, k, 1);
+        }
+    }
+}
+
 static int run_blocks(long long warps) {
     const long long b = (warps + kWarps - 1) / kWarps;
     return (int)(b > 1048576 ? 1048576 : (b < 1 ? 1 : b));
@@ -185,6 +299,59 @@ cudaError_t host_download(const BoxView& v, double* h, cudaStream_t st) {
 cudaError_t host_ghosts(const BoxView& v, double* h, cudaStream_t st) {
     const long long nw = (long long)(v.n[0] + 2 * CNS_NG) * (v.n[1] + 2 * CNS_NG) * ((v.n[2] + 2 * CNS_NG + kRun - 1) / kRun);
     k_host_ghosts<<<run_blocks(nw), kWarps * 32, 0, st>>>(v, h);
+    return cudaGetLastError();
+}
+
+// The queue of k_upload_deriv for a box with tile list `tiles` (see there).
+std::vector<int> upload_deriv_queue(const int n[3], const int tlog[3], const std::vector<Tile>& tiles) {
+    const int runs = (n[2] + kRun - 1) / kRun, per_plane = n[1] * runs;
+    const int items_per_plane = (per_plane + kWarps - 1) / kWarps;
+    std::vector<std::vector<int>> after(n[0]);  // tiles to place after plane order q
+    for (size_t t = 0; t < tiles.size(); t++) {
+        int lo, hi;
+        if (tlog[0] == kLinearTile) {
+            const long long plane = (long long)n[1] * n[2], last = (long long)n[0] * plane - 1;
+            const long long p0 = (long long)tiles[t].k0 * kTileThreads;
+            lo = (int)(p0 / plane);
+            hi = (int)(std::min(p0 + kTileThreads - 1, last) / plane);
+        } else {
+            lo = tiles[t].i0;
+            hi = std::min(tiles[t].i0 + (1 << tlog[0]), n[0]) - 1;
+        }
+        lo -= CNS_NG;
+        hi += CNS_NG;
+        int qmax = 0;
+        if (hi - lo >= n[0]) {
+            qmax = n[0] - 1;
+        } else {
+            for (int p = lo; p <= hi; p++) qmax = std::max(qmax, (((p % n[0]) + n[0]) % n[0] + kPlaneStart) % n[0]);
+        }
+        after[std::min(qmax + kDerivLag, n[0] - 1)].push_back(~(int)t);
+    }
+    std::vector<int> q;
+    q.reserve((size_t)n[0] * items_per_plane + tiles.size());
+    for (int p = 0; p < n[0]; p++) {
+        for (int it = 0; it < items_per_plane; it++) q.push_back(p * items_per_plane + it);
+        q.insert(q.end(), after[p].begin(), after[p].end());
+    }
+    return q;
+}
+
+cudaError_t host_upload_deriv(const BoxView& v, double* h, bool ghosts, const Tile* tiles, const int* queue, int nq,
+                              int* counters, cudaStream_t st) {
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const void* fn = ghosts ? (const void*)k_upload_deriv<true> : (const void*)k_upload_deriv<false>;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kWarps * 32, 0);
+    if (e != cudaSuccess) return e;
+    const int grid = std::max(1, nsm * per);
+    e = cudaMemsetAsync(counters, 0, sizeof(int) * (v.n[0] + 1), st);
+    if (e != cudaSuccess) return e;
+    if (ghosts)
+        k_upload_deriv<true><<<grid, kWarps * 32, 0, st>>>(v, h, tiles, queue, nq, counters + v.n[0], counters);
+    else
+        k_upload_deriv<false><<<grid, kWarps * 32, 0, st>>>(v, h, tiles, queue, nq, counters + v.n[0], counters);
     return cudaGetLastError();
 }
 

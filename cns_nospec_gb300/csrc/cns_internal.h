@@ -1,6 +1,8 @@
 // cns_internal.h -- launchers shared between the kernel files and the C ABI.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <vector>
 #include "cns_common.cuh"
 
 namespace cns {
@@ -49,6 +51,11 @@ void* mapped_host_range(const void* p, size_t bytes);
 cudaError_t host_upload(const BoxView& v, double* h, bool prim, bool ghosts, cudaStream_t st);
 cudaError_t host_download(const BoxView& v, double* h, cudaStream_t st);
 cudaError_t host_ghosts(const BoxView& v, double* h, cudaStream_t st);
+// the FP64 upload fused with stage 1's derivative pass (k_upload_deriv): its work queue for a
+// tile list, and the launch; counters = n[0] + 1 ints of device memory
+std::vector<int> upload_deriv_queue(const int n[3], const int tlog[3], const std::vector<Tile>& tiles);
+cudaError_t host_upload_deriv(const BoxView& v, double* h, bool ghosts, const Tile* tiles, const int* queue, int nq,
+                              int* counters, cudaStream_t st);
 cudaError_t op_init_field(const BoxView& b, double ax, double ay, double az, double perturb, unsigned long long seed,
                           cudaStream_t st);
 
