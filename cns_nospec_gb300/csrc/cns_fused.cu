@@ -60,6 +60,11 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
         double cour = 0.0;
         int health = 0;
+        // plain form, stage 3: the Courant number through FP32 candidates (below)
+        constexpr bool kDefer = sizeof(R) == 8 && STAGE == 3;
+        CourantInput64 cq;
+        float est = -1.0f;
+        bool inside = false;
         if (i < b.n[0] && j < b.n[1] && k < b.n[2]) {
             const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
             const R* Pr = (const R*)b.P[pr];
@@ -138,9 +143,35 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
                 }
             }
             if (STAGE == 3 && b.host_out) store_host(b, i, j, k, un);
-            cour = epilogue<R>(b, Pw, c, i, j, k, un, STAGE == 3, &health);
+            if (kDefer) {
+                epilogue_plain(b, (double*)Pw, c, i, j, k, un, &health, &cq);
+                est = courant_plain_est(b, cq);
+                inside = true;
+            } else {
+                cour = epilogue<R>(b, Pw, c, i, j, k, un, STAGE == 3, &health);
+            }
         }
         if (health) atomicOr(&b.sc->status, health);
+        if (kDefer) {
+            // The FP64 Courant number only where it can be the tile's maximum: with
+            // |est - exact| <= eps * exact (eps = 2^-20, over twice the estimate's bound), a cell
+            // whose estimate is below (1 - 2 eps) of the tile's largest is below that cell's exact
+            // value, so the maximum over the candidates is the maximum over the tile, bit for
+            // bit.  NaN or tiny estimates are always candidates, and all cells are when an
+            // estimate overflowed.  Warps without a candidate skip the FP64 code.
+            __shared__ float s_max[kTileThreads / 32];
+            float m = est;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+            __syncthreads();
+            m = s_max[0];
+#pragma unroll
+            for (int q = 1; q < kTileThreads / 32; q++) m = fmaxf(m, s_max[q]);
+            __syncthreads();  // s_max is rewritten for the next tile
+            const float thr = m * (1.0f - 0x1p-18f);
+            if (inside && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f))) cour = courant_plain(b, cq);
+        }
         if (STAGE == 3) courant_fold(b, cour);
     }
 }

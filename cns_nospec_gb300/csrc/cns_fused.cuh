@@ -153,9 +153,40 @@ template <class R>
 __device__ __forceinline__ double epilogue(const BoxView& b, R* __restrict__ Pw, long long c, int i, int j, int k,
                                            const double un[5], bool want_cour, int* health);
 
+// What the plain form's Courant number of a cell is formed from (cpu/ctoprim.cpp:50-69).
+struct CourantInput64 {
+    double p, rinv, u, v, w;
+};
+__device__ __forceinline__ double courant_plain(const BoxView& b, const CourantInput64& q) {
+    const double cs = sqrt((kGamma * q.p) * q.rinv);
+    const double cx = (cs + fabs(q.u)) * b.c64.cour[0];
+    const double cy = (cs + fabs(q.v)) * b.c64.cour[1];
+    const double cz = (cs + fabs(q.w)) * b.c64.cour[2];
+    return fmax(fmax(cx, cy), cz);
+}
+// An FP32 estimate of courant_plain: counting 2^-24 per rounding (p, 1/rho, u, 1.4, two
+// products, sqrt, the sum, 1/dx, the last product) it lies within ~7 * 2^-24 of it for states
+// whose values are normal FP32 numbers.
+__device__ __forceinline__ float courant_plain_est(const BoxView& b, const CourantInput64& q) {
+    const float cs = sqrtf(1.4f * (float)q.p * (float)q.rinv);
+    const float cx = (cs + fabsf((float)q.u)) * b.c32.cour[0];
+    const float cy = (cs + fabsf((float)q.v)) * b.c32.cour[1];
+    const float cz = (cs + fabsf((float)q.w)) * b.c32.cour[2];
+    return fmaxf(fmaxf(cx, cy), cz);
+}
+
+// The plain form's epilogue without the Courant number, whose inputs it leaves in *q.
+__device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restrict__ Pw, long long c, int i, int j,
+                                               int k, const double un[5], int* health, CourantInput64* q);
 template <>
 __device__ __forceinline__ double epilogue<double>(const BoxView& b, double* __restrict__ Pw, long long c, int i,
                                                    int j, int k, const double un[5], bool want_cour, int* health) {
+    CourantInput64 q;
+    epilogue_plain(b, Pw, c, i, j, k, un, health, &q);
+    return want_cour ? courant_plain(b, q) : 0.0;
+}
+__device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restrict__ Pw, long long c, int i, int j,
+                                               int k, const double un[5], int* health, CourantInput64* q) {
     const long long fs = b.fs;
     const double rho = un[0], mx = un[1], my = un[2], mz = un[3], E = un[4];
     const double rinv = rcp_nr(rho);
@@ -182,12 +213,7 @@ __device__ __forceinline__ double epilogue<double>(const BoxView& b, double* __r
     store_img(Pw + PHU * fs, b, c, i, j, k, H * u, 1);
     store_img(Pw + PHV * fs, b, c, i, j, k, H * v, 2);
     store_img(Pw + PHW * fs, b, c, i, j, k, H * w, 4);
-    if (!want_cour) return 0.0;
-    const double cs = sqrt((kGamma * p) * rinv);
-    const double cx = (cs + fabs(u)) * b.c64.cour[0];
-    const double cy = (cs + fabs(v)) * b.c64.cour[1];
-    const double cz = (cs + fabs(w)) * b.c64.cour[2];
-    return fmax(fmax(cx, cy), cz);
+    *q = CourantInput64{p, rinv, u, v, w};
 }
 
 // The mixed form's reference values (fixed per box).  A loop over cells loads them once: read
