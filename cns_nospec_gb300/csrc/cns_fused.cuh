@@ -93,6 +93,35 @@ __device__ __forceinline__ void store_img(R* __restrict__ f, const BoxView& b, l
     }
 }
 
+// The axes along which each P field's stencils difference it (1 = i, 2 = j, 4 = k): the
+// periodic face images it needs.
+__host__ __device__ constexpr int pimg(int f) {
+    return f <= PT ? 7 : (f == PFUV ? 3 : (f == PFUW ? 5 : (f == PFVW ? 6 : 1 << ((f - PMX) % 3))));
+}
+
+// Store the 16 P fields of cell (i, j, k), then the face images of those that need them.  Most
+// cells need none; i and j are the same across a warp (so those branches do not diverge), and
+// only the lanes within 4 cells of a k face take the k branch.  The same stores as store_img
+// field by field; images lie in the ghost layers, so the order does not matter.
+template <class R>
+__device__ __forceinline__ void store_pset(R* __restrict__ Pw, const BoxView& b, long long c, int i, int j, int k,
+                                           const R (&v)[NPF]) {
+    const long long fs = b.fs;
+#pragma unroll
+    for (int f = 0; f < NPF; f++) Pw[f * fs + c] = v[f];
+    auto images = [&](int axis, long long d) {
+#pragma unroll
+        for (int f = 0; f < NPF; f++)
+            if (pimg(f) & axis) Pw[f * fs + c + d] = v[f];
+    };
+    if (i < CNS_NG) images(1, (long long)b.n[0] * b.si);
+    if (i >= b.n[0] - CNS_NG) images(1, -(long long)b.n[0] * b.si);
+    if (j < CNS_NG) images(2, (long long)b.n[1] * b.sj);
+    if (j >= b.n[1] - CNS_NG) images(2, -(long long)b.n[1] * b.sj);
+    if (k < CNS_NG) images(4, b.n[2]);
+    if (k >= b.n[2] - CNS_NG) images(4, -b.n[2]);
+}
+
 // Stage 3 of a step whose result goes straight to the caller's page-locked host array
 // (BoxView::host_out): the cell's new state at U[i+4][j+4][k+4][0..4] of the reference layout,
 // written over the CPU-GPU link while the kernel computes.
@@ -197,6 +226,8 @@ __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restr
     const double T = eint * (1.0 / kCv);
     const double H = E + p;
     *health |= health_bits(rho, eint);
+    // Field by field, not store_pset: its 16 live FP64 values would cost the upload kernels
+    // occupancy, and the FP64-bound kernels gain nothing from fewer store instructions.
     store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
     store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
     store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
@@ -269,7 +300,6 @@ __device__ __forceinline__ double epilogue<float>(const BoxView& b, float* __res
 __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
                                                  int k, const double un[5], bool want_cour, int* health,
                                                  const MixedRefs& sc, CourantInput* ci) {
-    const long long fs = b.fs;
     const double rho = un[0], E = un[4];
     const float rhof = (float)rho;
     const float rf = 1.0f / rhof;
@@ -287,22 +317,9 @@ __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __rest
     const float dT = (float)((eint - sc.e) * (1.0 / kCv));  // T - T_ref
     const float dH = (float)(E - sc.E) + dp;                // (E + p) - H_ref
     *health |= health_bits(rho, eint);
-    store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
-    store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
-    store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
-    store_img(Pw + PT * fs, b, c, i, j, k, dT, 7);
-    store_img(Pw + PMX * fs, b, c, i, j, k, mx, 1);
-    store_img(Pw + PMY * fs, b, c, i, j, k, my, 2);
-    store_img(Pw + PMZ * fs, b, c, i, j, k, mz, 4);
-    store_img(Pw + PFUU * fs, b, c, i, j, k, fmaf(mx, u, dp), 1);
-    store_img(Pw + PFVV * fs, b, c, i, j, k, fmaf(my, v, dp), 2);
-    store_img(Pw + PFWW * fs, b, c, i, j, k, fmaf(mz, w, dp), 4);
-    store_img(Pw + PFUV * fs, b, c, i, j, k, mx * v, 3);
-    store_img(Pw + PFUW * fs, b, c, i, j, k, mx * w, 5);
-    store_img(Pw + PFVW * fs, b, c, i, j, k, my * w, 6);
-    store_img(Pw + PHU * fs, b, c, i, j, k, dH * u, 1);
-    store_img(Pw + PHV * fs, b, c, i, j, k, dH * v, 2);
-    store_img(Pw + PHW * fs, b, c, i, j, k, dH * w, 4);
+    const float pv[NPF] = {u, v, w, dT, mx, my, mz, fmaf(mx, u, dp), fmaf(my, v, dp), fmaf(mz, w, dp),
+                           mx * v, mx * w, my * w, dH * u, dH * v, dH * w};
+    store_pset(Pw, b, c, i, j, k, pv);
     if (ci) {
         ci->p = pd + sc.p;
         ci->est = courant_mixed_est(b, rf, u, v, w, (float)ci->p);
