@@ -52,9 +52,10 @@ def parse():
     p.add_argument("--case", choices=["fp64", "mixed", "e2e"], default=None,
                    help="profiling case: only upload + warmup + steps of one form (for ncu), then exit; "
                         "e2e: warmup + steps calls of cns_new_advance on a page-locked host array")
-    p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve"], default="box",
+    p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve", "cpu"], default="box",
                    help="box: the headline 128^3 line (default); batch: 256 uneven boxes; "
-                        "mixed256: FP64 vs mixed at --size (use 256); serve: the request stream")
+                        "mixed256: FP64 vs mixed at --size (use 256); serve: the request stream; "
+                        "cpu: the CPU baseline table (the oracle port on the host cores)")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     p.add_argument("--boxes", type=int, default=256)
     p.add_argument("--rate", type=float, default=3.0, help="serve: requests per second")
@@ -202,6 +203,53 @@ def cpu_baseline(n: int, seconds: float):
     return {"value": n ** 3 * steps / el, "unit": "cell-updates/s", "cores": threads, "kind": "port",
             "sample": f"{steps} RK3 step(s) of the {n}^3 box, {threads} OpenMP threads, {el:.1f} s",
             "one_core_by_n": one, "reference_lib_present": which == "ref"}
+
+
+def _cpu_process(n, steps):
+    """One single-threaded oracle run (a child process of run_cpu_table)."""
+    from cns_nospec_gb300 import initdata as I
+    from oracle import oracle as O
+    O.set_threads(1)
+    U = I.initial_state(n, perturb=1e-3, seed=1)
+    t0 = time.perf_counter()
+    O.advance(U, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
+    return time.perf_counter() - t0
+
+
+def run_cpu_table(args):
+    """The CPU baseline in full: the oracle port (the reference's cpu/ algorithm, same operation
+    order) on one core at 32^3 (10 steps), 128^3 and 256^3 (3 steps); on all host cores as one
+    OpenMP process; and as one single-threaded process per core, each advancing its own 128^3
+    box (aggregate = all processes' cell-updates / the wall time of the slowest)."""
+    import multiprocessing as mp
+    from cns_nospec_gb300 import initdata as I
+    from oracle import oracle as O
+    O.build(ref=False)
+    cores = os.cpu_count() or 1
+    one = {}
+    O.set_threads(1)
+    for n, steps in ((32, 10), (128, 3), (256, 3)):
+        U = I.initial_state(n, perturb=1e-3, seed=1)
+        t0 = time.perf_counter()
+        O.advance(U, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
+        one[str(n)] = n ** 3 * steps / (time.perf_counter() - t0)
+    threads = {}
+    O.set_threads(cores)
+    for n, steps in ((128, 10), (256, 3)):
+        U = I.initial_state(n, perturb=1e-3, seed=1)
+        t0 = time.perf_counter()
+        O.advance(U, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
+        threads[str(n)] = n ** 3 * steps / (time.perf_counter() - t0)
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        times = pool.starmap(_cpu_process, [(128, 3)] * cores)
+    wall = time.perf_counter() - t0
+    return {"workload": "CPU baseline: the oracle port of the reference's cpu/ path, sinusoidal field with a 1e-3 "
+                        "perturbation (seed 1)", "unit": "cell-updates/s", "cores": cores,
+            "one_core_by_n": one, "openmp_all_cores_by_n": threads,
+            "processes_128": {"processes": cores, "steps_each": 3, "aggregate": cores * 128 ** 3 * 3 / max(times),
+                              "wall_s_incl_startup": wall, "per_process_s": [round(t, 2) for t in times]}}
 
 
 def run_reference(args, dist):
@@ -564,7 +612,7 @@ def main():
         run_case(args)
         return
     if args.workload != "box":
-        fn = {"batch": run_batch, "mixed256": run_mixed256, "serve": run_serve}[args.workload]
+        fn = {"batch": run_batch, "mixed256": run_mixed256, "serve": run_serve, "cpu": run_cpu_table}[args.workload]
         print(json.dumps(fn(args)))
         return
     dist = Dist()
