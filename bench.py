@@ -171,21 +171,36 @@ def measured_traffic(kernel: str, n: int):
 
 
 # ---- CPU baseline: the oracle (the reference's algorithm restated in C) on the host cores ----
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform string)."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
 def cpu_baseline(n: int, seconds: float):
+    """The reference algorithm (the oracle port, the reference's cpu/ operation order) on the
+    host cores: one single-threaded process per core, each advancing its own n^3 box, for about
+    `seconds` (oracle_processes); beside it one core alone at 32^3 and n^3, and all cores as one
+    OpenMP process on one box."""
     from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
     O.build(ref=os.path.isdir(O.REF_SRC))
-    which = "ref" if (O.have_ref() and os.path.isdir(O.REF_SRC)) else "port"
-    threads = O.set_threads(os.cpu_count() or 1)
-    U = I.initial_state(n, perturb=1e-3, seed=1)
-    dx = I.box_dx(n)
-    steps, t0 = 0, time.perf_counter()
-    while True:
-        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which="port")
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds or steps >= 100:
-            break
+    cores = os.cpu_count() or 1
+    value, steps, wall = oracle_processes(n, 100, 1, seconds, cores)
     # one core, as the reference's own cpu/ path runs (its OpenMP pragmas are commented out)
     one = {}
     O.set_threads(1)
@@ -199,29 +214,71 @@ def cpu_baseline(n: int, seconds: float):
             if e1 >= budget or k >= 50:
                 break
         one[str(m)] = m ** 3 * k / e1
-    O.set_threads(threads)
-    return {"value": n ** 3 * steps / el, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} RK3 step(s) of the {n}^3 box, {threads} OpenMP threads, {el:.1f} s",
-            "one_core_by_n": one, "reference_lib_present": which == "ref"}
+    threads = O.set_threads(cores)
+    U = I.initial_state(n, perturb=1e-3, seed=1)
+    k, t1 = 0, time.perf_counter()
+    while True:
+        U, _ = O.advance(U, 1, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
+        k += 1
+        e1 = time.perf_counter() - t1
+        if e1 >= 4.0 or k >= 20:
+            break
+    return {"value": value, "unit": "cell-updates/s", "cores": cores, "cpu_model": cpu_model(), "kind": "port",
+            "sample": f"{cores} single-threaded processes, {steps} RK3 steps in all of their own {n}^3 boxes, "
+                      f"{wall:.1f} s", "one_core_by_n": one,
+            "openmp_one_process": {"value": n ** 3 * k / e1, "threads": threads, "steps": k}}
 
 
-def _cpu_process(n, steps):
-    """One single-threaded oracle run (a child process of run_cpu_table)."""
+def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
+    """One single-threaded run of the reference algorithm (a child process of oracle_processes):
+    `warmup` untimed steps, a barrier with the other processes, then up to `steps` timed steps or
+    `seconds` of them.  Puts the steps done and the wall-clock start and end of the timed part."""
     from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
     O.set_threads(1)
     U = I.initial_state(n, perturb=1e-3, seed=1)
-    t0 = time.perf_counter()
-    O.advance(U, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
-    return time.perf_counter() - t0
+    dx = I.box_dx(n)
+    for _ in range(warmup):
+        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
+    barrier.wait(timeout=600)
+    k, t0 = 0, time.time()
+    while k < steps:
+        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
+        k += 1
+        if time.time() - t0 >= seconds:
+            break
+    out.put((k, t0, time.time()))
+
+
+def oracle_processes(n, steps, warmup, seconds, nproc, which="port"):
+    """The reference algorithm on every host core the way its single-threaded cpu/ code uses
+    them: `nproc` independent processes (spawned), each advancing its own copy of the n^3 box,
+    their timed parts started together.  Throughput = all processes' cell-updates / (last end -
+    first start)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    barrier, out = ctx.Barrier(nproc), ctx.Queue()
+    procs = [ctx.Process(target=_oracle_process, args=(n, steps, warmup, seconds, which, barrier, out))
+             for _ in range(nproc)]
+    for p in procs:
+        p.start()
+    try:
+        res = [out.get(timeout=900) for _ in procs]
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+    if any(p.exitcode != 0 for p in procs):
+        raise RuntimeError("an oracle process failed")
+    done = sum(r[0] for r in res)
+    wall = max(r[2] for r in res) - min(r[1] for r in res)
+    return n ** 3 * done / wall, done, wall
 
 
 def run_cpu_table(args):
     """The CPU baseline in full: the oracle port (the reference's cpu/ algorithm, same operation
     order) on one core at 32^3 (10 steps), 128^3 and 256^3 (3 steps); on all host cores as one
     OpenMP process; and as one single-threaded process per core, each advancing its own 128^3
-    box (aggregate = all processes' cell-updates / the wall time of the slowest)."""
-    import multiprocessing as mp
+    box (oracle_processes)."""
     from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
     O.build(ref=False)
@@ -240,54 +297,39 @@ def run_cpu_table(args):
         t0 = time.perf_counter()
         O.advance(U, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
         threads[str(n)] = n ** 3 * steps / (time.perf_counter() - t0)
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        times = pool.starmap(_cpu_process, [(128, 3)] * cores)
-    wall = time.perf_counter() - t0
+    agg, done, wall = oracle_processes(128, 3, 0, 1e9, cores)
     return {"workload": "CPU baseline: the oracle port of the reference's cpu/ path, sinusoidal field with a 1e-3 "
-                        "perturbation (seed 1)", "unit": "cell-updates/s", "cores": cores,
+                        "perturbation (seed 1)", "unit": "cell-updates/s", "cores": cores, "cpu_model": cpu_model(),
             "one_core_by_n": one, "openmp_all_cores_by_n": threads,
-            "processes_128": {"processes": cores, "steps_each": 3, "aggregate": cores * 128 ** 3 * 3 / max(times),
-                              "wall_s_incl_startup": wall, "per_process_s": [round(t, 2) for t in times]}}
+            "processes_128": {"processes": cores, "steps_each": 3, "aggregate": agg, "wall_s": wall}}
 
 
 def run_reference(args, dist):
-    """--impl reference: the reference algorithm (the oracle port; the reference's own objects
-    cannot be rebuilt where its source tree is absent) on the host cores, same workload."""
+    """--impl reference: the reference algorithm on the host cores, same workload.  Where the
+    reference tree exists its own cpu/ objects run (oracle/_ref); elsewhere (the GPU machine, where
+    it is absent and x86 objects do not travel) the oracle port, which gives the same bits.
+    Its cpu/ path is single-threaded, so it uses the cores as one process per core, each
+    advancing its own copy of the box (oracle_processes): `warmup` untimed steps, then `steps`
+    timed steps, bounded to about a minute."""
     if dist.rank != 0:
         return None
-    from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
     O.build(ref=os.path.isdir(O.REF_SRC))
     use_ref = O.have_ref() and os.path.isdir(O.REF_SRC)
-    threads = O.set_threads(os.cpu_count() or 1)
-    n = args.n
-    U = I.initial_state(n, perturb=1e-3, seed=1)
-    dx = I.box_dx(n)
     which = "ref" if use_ref else "port"
-    if use_ref:
-        threads = 1  # the reference's cpu/ path is single-threaded (its OpenMP pragmas are commented out)
-    for _ in range(min(args.warmup, 1)):
-        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
-    # bounded sample: at most ~120 s of timed work
-    t0 = time.perf_counter()
-    steps = 0
-    while steps < args.steps:
-        U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
-        steps += 1
-        if time.perf_counter() - t0 > 120.0:
-            break
-    el = time.perf_counter() - t0
-    v = n ** 3 * steps / el
+    cores = os.cpu_count() or 1
+    n = args.n
+    warm = min(args.warmup, 1)
+    v, done, wall = oracle_processes(n, args.steps, warm, 60.0, cores, which=which)
+    steps = max(1, done // cores)
     kind = "reference" if use_ref else "port"
+    sample = f"{cores} single-threaded processes x {steps} RK3 steps of their own {n}^3 box, {wall:.1f} s"
     return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * wall / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": box_workload(n), "n": n,
-                       "host_threads": threads},
-            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind,
-                             "sample": f"{steps} RK3 steps of the {n}^3 box on the host cores"},
+            "config": {"workload": box_workload(n), "n": n, "host_processes": cores},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "cpu_model": cpu_model(), "kind": kind,
+                             "sample": sample},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
