@@ -561,10 +561,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
 // One 512-thread block per SM: warps 0-7 (the stencil group) run the 20 TMA-fed field phases of
 // tile t while warps 8-15 (the write-back group) run the FP64 write-back of tile t-1, so the
 // FP32 stencils and the FP64 write-back overlap instead of alternating.  The fields are
-// double-buffered (a third buffer measured slower: 200 KB of shared memory leaves too little
-// L1).  The sums move between the
-// groups through two 40 KB stash slots: full[s] (256 stencil arrivals) hands slot s to the
-// write-back group, empty[s] (256 write-back arrivals) hands it back.  The stencil group
+// double-buffered, and the sums move between the groups through one 40 KB stash slot: full
+// (256 stencil arrivals) hands it to the write-back group, empty (256 write-back arrivals)
+// hands it back.  120 KB of shared memory leave the most L1 for the write-back's state loads:
+// a second slot (160 KB) measured 0.5-1 % slower, and a third field buffer with two slots
+// (200 KB) 10-15 % slower; the code takes any kWsBufs / kWsSlots.  The stencil group
 // synchronises on named barrier 1 only (once per field); the write-back group needs no barrier.
 // Every wait is bounded.  A stencil thread whose wait gives up stops waiting and computing but
 // keeps taking part in the barrier and the hand-over, so no thread is ever left waiting on it;
@@ -575,7 +576,8 @@ constexpr int kWsThreads = 2 * kTileThreads;
 constexpr int kStashElems = 5 * XI * kTileThreads;  // 10240 floats
 static_assert(kStashElems == kBufElems, "a stash slot is one field buffer in size");
 
-constexpr int kWsBufs = 2;
+constexpr int kWsBufs = 2;   // field buffers
+constexpr int kWsSlots = 1;  // stash slots
 __device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
 template <int STAGE>
@@ -583,15 +585,15 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
                                                             const Tile* __restrict__ tiles, int ntiles) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* buf = (float*)smem_raw;                                // kWsBufs field buffers
-    float* stash = buf + kWsBufs * kBufElems;                     // 2 stash slots
-    uint64_t* bar = (uint64_t*)(stash + 2 * kStashElems);         // TMA[kWsBufs], full[2], empty[2]
+    float* stash = buf + kWsBufs * kBufElems;                     // kWsSlots stash slots
+    uint64_t* bar = (uint64_t*)(stash + kWsSlots * kStashElems);  // TMA[kWsBufs], full[kWsSlots], empty[kWsSlots]
     uint64_t* full = bar + kWsBufs;
-    uint64_t* empty = full + 2;
+    uint64_t* empty = full + kWsSlots;
     const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     if (my_tiles <= 0) return;
     if (threadIdx.x == 0) {
         for (int q = 0; q < kWsBufs; q++) mbar_init(&bar[q]);
-        for (int q = 0; q < 2; q++) {
+        for (int q = 0; q < kWsSlots; q++) {
             mbar_init_n(&full[q], kTileThreads);
             mbar_init_n(&empty[q], kTileThreads);
         }
@@ -605,8 +607,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
         for (int it = 0; it < my_tiles; it++) {
             const Tile T = tiles[blockIdx.x + it * gridDim.x];
             const BoxView& b = boxes[T.box];
-            const int slot = it & 1;
-            const bool ok = mbar_wait_bounded(&full[slot], (uint32_t)((it >> 1) & 1));
+            const int slot = it % kWsSlots;
+            const bool ok = mbar_wait_bounded(&full[slot], (uint32_t)((it / kWsSlots) & 1));
             if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform, so the shuffles below stay whole
                 if ((wt & 31) == 0) atomicOr(&b.sc->status, HEALTH_TIMEOUT);
                 return;
@@ -650,9 +652,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
             if (!bad) consume_field(e, buf + (g % kWsBufs) * kBufElems, T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
             group_sync();  // buffer g % kWsBufs is free for load g + kWsBufs
         }
-        // hand the sums over: slot it & 1, once the write-back of tile it - 2 has released it
-        const int slot = it & 1;
-        if (it >= 2 && !bad && !mbar_wait_bounded(&empty[slot], (uint32_t)(((it >> 1) - 1) & 1))) {
+        // hand the sums over: slot it % kWsSlots, once the write-back of tile it - kWsSlots has released it
+        const int slot = it % kWsSlots;
+        if (it >= kWsSlots && !bad && !mbar_wait_bounded(&empty[slot], (uint32_t)(((it / kWsSlots) - 1) & 1))) {
             bad = true;
             bad_status = &b.sc->status;
         }
@@ -876,7 +878,8 @@ cudaError_t launch_deriv_tma(const BoxView* boxes, const Tile* tiles, int ntiles
     return cudaGetLastError();
 }
 
-constexpr size_t kWsSmem = (kWsBufs * kBufElems + 2 * kStashElems) * sizeof(float) + (kWsBufs + 4) * sizeof(uint64_t);
+constexpr size_t kWsSmem =
+    (kWsBufs * kBufElems + kWsSlots * kStashElems) * sizeof(float) + (kWsBufs + 2 * kWsSlots) * sizeof(uint64_t);
 
 template <int STAGE>
 static cudaError_t launch_ws_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
@@ -888,7 +891,7 @@ static cudaError_t launch_ws_stage(const BoxView* boxes, const Tile* tiles, int 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kWsThreads, kWsSmem);
     if (e != cudaSuccess) return e;
-    if (per < 1) return cudaErrorInvalidConfiguration;  // 512 threads x 128 registers and 160 KB must fit
+    if (per < 1) return cudaErrorInvalidConfiguration;  // 512 threads x 128 registers and kWsSmem must fit
     const int grid = ntiles < nsm * per ? ntiles : nsm * per;
     fn<<<grid, kWsThreads, kWsSmem, st>>>(boxes, tiles, ntiles);
     return cudaGetLastError();
