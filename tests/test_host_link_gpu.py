@@ -107,3 +107,23 @@ def test_named_entry_points_equal_advance_host(gpu, cns, precision):
     dts = np.zeros(2)
     L.check(fn(L.dptr(b), L.iarr(list(n)), L.darr(I.box_dx(n)), I.CFL, I.ETA, I.ALAM, 2, L.dptr(dts)))
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_offset_inside_larger_pinned_allocation(gpu, cns):
+    """U as the second of two arrays carved from one page-locked allocation: in place, and the
+    first array (outside U's range) is left untouched."""
+    from cns_nospec_gb300 import initdata as I
+    n = (12, 16, 20)
+    U0 = garbage_ghosts(I.initial_state(n, perturb=1e-3, seed=13), 4)
+    t = torch.empty((2,) + U0.shape, dtype=torch.float64, pin_memory=True)
+    both = t.numpy()
+    both[0] = 7.0
+    both[1] = U0
+    Ub = both[1]
+    assert Ub.flags.c_contiguous and in_place(gpu, Ub) == 1
+    Ua = U0.copy()
+    dta = cns.advance_host(Ua, 2, I.box_dx(n), I.CFL, I.ETA, I.ALAM, 0)
+    dtb = cns.advance_host(Ub, 2, I.box_dx(n), I.CFL, I.ETA, I.ALAM, 0)
+    assert np.array_equal(dta, dtb)
+    assert np.array_equal(Ua.view(np.uint64), Ub.view(np.uint64))
+    assert np.all(both[0] == 7.0)
