@@ -7,7 +7,7 @@ normwise relative error per conserved variable <= 1e-12 (FP64_TOL)."""
 import numpy as np
 import pytest
 
-from conftest import FP64_TOL, golden, normwise
+from conftest import FP64_TOL, MIXED_TOL, golden, normwise
 from cns_nospec_gb300 import initdata as I
 
 pytestmark = pytest.mark.gpu
@@ -126,6 +126,25 @@ def test_advance_perturbed_128cube_100_steps(gpu, cns, oracle):
     assert err.max() <= FP64_TOL, err
     dt, steps = box.last_dt()
     assert steps == 100 and abs(dt - rdt[-1]) <= 1e-12 * rdt[-1]
+
+
+def test_advance_256cube_3_steps(gpu, cns, oracle):
+    """256^3 (the mixed-form comparison size), 3 RK3 steps against the oracle run live: the FP64
+    form within FP64_TOL, the mixed form within MIXED_TOL."""
+    n = 256
+    U0 = I.initial_state(n, perturb=1e-3, seed=1)
+    ref, rdt = oracle.advance(U0, 3, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    for prec, tol in ((cns.CNS_FP64, FP64_TOL), (cns.CNS_MIXED, MIXED_TOL)):
+        box = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
+        try:
+            box.upload(U0)
+            box.advance(3)
+            box.sync()
+            U = box.download()
+        finally:
+            box.close()
+        err = normwise(U, ref)
+        assert err.max() <= tol, (prec, err)
 
 
 def test_resident_box_equals_host_path_bitwise(gpu, cns):
