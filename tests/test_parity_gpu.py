@@ -1,8 +1,9 @@
 """Parity of the GPU library (called through the C ABI) with the reference's cpu/ path.
 
 Small cases compare against the committed golden fixtures (made by the reference itself) and
-against the oracle run live on identical inputs; full-size cases check properties that do
-not need the oracle (bitwise periodic shift-equivariance, mass conservation).  Tolerance:
+against the oracle run live on identical inputs, up to 128^3 x 100 steps and 256^3 x 3 steps;
+full-size cases also check properties that do not need the oracle (bitwise periodic
+shift-equivariance, mass conservation).  Tolerance:
 normwise relative error per conserved variable <= 1e-12 (FP64_TOL)."""
 import numpy as np
 import pytest
