@@ -262,13 +262,20 @@ def oracle_processes(n, steps, warmup, seconds, nproc, which="port"):
              for _ in range(nproc)]
     for p in procs:
         p.start()
+    import queue
+    res, t0 = [], time.time()
     try:
-        res = [out.get(timeout=900) for _ in procs]
+        while len(res) < nproc:
+            try:
+                res.append(out.get(timeout=5))
+            except queue.Empty:
+                if any(p.exitcode not in (None, 0) for p in procs) or time.time() - t0 > 900:
+                    raise RuntimeError("an oracle process failed or did not finish")
     finally:
         for p in procs:
             p.join(timeout=60)
-    if any(p.exitcode != 0 for p in procs):
-        raise RuntimeError("an oracle process failed")
+            if p.is_alive():
+                p.terminate()
     done = sum(r[0] for r in res)
     wall = max(r[2] for r in res) - min(r[1] for r in res)
     return n ** 3 * done / wall, done, wall
