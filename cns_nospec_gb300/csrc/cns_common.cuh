@@ -151,13 +151,15 @@ __host__ __device__ inline long long cell_off(const BoxView& b, int i, int j, in
 // Positive doubles order like their bit patterns; the Courant max uses integer atomics.
 __device__ inline unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 
-// Reciprocal for FP64: an FP32 seed refined by one third-order Newton-series step
-// r <- r (1 + e + e^2), e = 1 - x r (Householder's method of order 3 for 1/x).  The seed's
-// relative error e0 ~ 1e-7 becomes ~e0^3, so the result is within a few ulp of 1/x for
-// normal FP32-representable x (the densities here are ~1e-3).  Costs three FP64 FMAs
-// instead of a full IEEE division.
+// Reciprocal for FP64: the PTX approximate reciprocal (rcp.approx.ftz.f64, special-function
+// unit) as the seed, refined by one third-order Newton-series step r <- r (1 + e + e^2),
+// e = 1 - x r (Householder's method of order 3 for 1/x).  The seed's relative error e0 (a
+// single-precision-level approximation) becomes ~e0^3, so the result is within a few ulp of
+// 1/x.  Costs three FP64 FMAs instead of a full IEEE division, and no FP32<->FP64 conversion
+// (those issue to the FP64 pipe).
 __device__ inline double rcp_nr(double x) {
-    double r = (double)(1.0f / (float)x);
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
     double e = fma(-x, r, 1.0);
     return fma(r, fma(e, e, e), r);
 }

@@ -154,11 +154,12 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
         if (health) atomicOr(&b.sc->status, health);
         if (kDefer) {
             // The FP64 Courant number only where it can be the tile's maximum: with
-            // |est - exact| <= eps * exact (eps = 2^-20, over twice the estimate's bound), a cell
-            // whose estimate is below (1 - 2 eps) of the tile's largest is below that cell's exact
-            // value, so the maximum over the candidates is the maximum over the tile, bit for
-            // bit.  NaN or tiny estimates are always candidates, and all cells are when an
-            // estimate overflowed.  Warps without a candidate skip the FP64 code.
+            // |est - exact| <= eps * exact (eps = kCourantPlainEps = 2^-18, over twice the
+            // estimate's bound), a cell whose estimate is below (1 - 4 eps) of the tile's largest
+            // (below (1 - eps) / (1 + eps) of it, with margin) is below the exact value of that
+            // largest estimate's cell, so the maximum over the candidates is the maximum over
+            // the tile, bit for bit.  NaN or tiny estimates are always candidates, and all cells
+            // are when an estimate overflowed.  Warps without a candidate skip the FP64 code.
             __shared__ float s_max[kTileThreads / 32];
             float m = est;
 #pragma unroll
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
 #pragma unroll
             for (int q = 1; q < kTileThreads / 32; q++) m = fmaxf(m, s_max[q]);
             __syncthreads();  // s_max is rewritten for the next tile
-            const float thr = m * (1.0f - 0x1p-18f);
+            const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
             if (inside && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f))) cour = courant_plain(b, cq);
         }
         if (STAGE == 3) courant_fold(b, cour);

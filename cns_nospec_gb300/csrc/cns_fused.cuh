@@ -193,14 +193,26 @@ __device__ __forceinline__ double courant_plain(const BoxView& b, const CourantI
     const double cz = (cs + fabs(q.w)) * b.c64.cour[2];
     return fmax(fmax(cx, cy), cz);
 }
-// An FP32 estimate of courant_plain: counting 2^-24 per rounding (p, 1/rho, u, 1.4, two
-// products, sqrt, the sum, 1/dx, the last product) it lies within ~7 * 2^-24 of it for states
-// whose values are normal FP32 numbers.
+// A double cut to FP32 on the integer pipes: its sign, exponent and top 20 mantissa bits
+// (relative error below 2^-20, toward zero); zero stays zero, and anything else outside the
+// normal FP32 range becomes NaN.  Hardware conversions would issue to the FP64 pipe, the bound
+// of the plain kernels.
+__device__ __forceinline__ float f32_cut(double d) {
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    if (((hi >> 20) & 0x7FFu) - 897u < 254u)
+        return __uint_as_float((hi & 0x80000000u) | (((hi & 0x7FFFFFFFu) << 3) - 0xC0000000u));
+    return __uint_as_float((((hi & 0x7FFFFFFFu) | lo) == 0u) ? (hi & 0x80000000u) : 0x7FC00000u);
+}
+// An FP32 estimate of courant_plain from those cut inputs: counting 2^-20 per cut input and
+// 2^-24 per FP32 rounding (1.4, two products, sqrt, the sum, 1/dx, the last product) it lies
+// within ~1.4 * 2^-20 of it (courant_eps is 2^-18) for states whose values are normal FP32
+// numbers; outside that range it is NaN.
+constexpr float kCourantPlainEps = 0x1p-18f;
 __device__ __forceinline__ float courant_plain_est(const BoxView& b, const CourantInput64& q) {
-    const float cs = sqrtf(1.4f * (float)q.p * (float)q.rinv);
-    const float cx = (cs + fabsf((float)q.u)) * b.c32.cour[0];
-    const float cy = (cs + fabsf((float)q.v)) * b.c32.cour[1];
-    const float cz = (cs + fabsf((float)q.w)) * b.c32.cour[2];
+    const float cs = sqrtf(1.4f * f32_cut(q.p) * f32_cut(q.rinv));
+    const float cx = (cs + fabsf(f32_cut(q.u))) * b.c32.cour[0];
+    const float cy = (cs + fabsf(f32_cut(q.v))) * b.c32.cour[1];
+    const float cz = (cs + fabsf(f32_cut(q.w))) * b.c32.cour[2];
     return fmaxf(fmaxf(cx, cy), cz);
 }
 

@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_upload_deriv(BoxView b, double*
                                                                int* done) {
     __shared__ double s[kWarps][kRun * CNS_NC];
     __shared__ int s_item, s_ok;
+    __shared__ float s_max[kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double* sw = s[warp];
     const int runs = (b.n[2] + kRun - 1) / kRun, per_plane = b.n[1] * runs;
@@ -205,18 +206,20 @@ __global__ void __launch_bounds__(kWarps * 32) k_upload_deriv(BoxView b, double*
         if (item == INT_MIN) return;
         if (item >= 0) {  // upload: run (item % items_per_plane) * 8 + warp of plane order q
             const int q = item / items_per_plane, rr = (item % items_per_plane) * kWarps + warp;
-            if (rr >= per_plane) continue;  // warp-uniform; the next block barrier is at the loop top
+            const bool has = rr < per_plane;  // warp-uniform; warps without a run still join the barriers
             RunIdx r;
             r.i = (q + b.n[0] - kPlaneStart) % b.n[0];
             r.j = rr / runs;
             r.k0 = (rr % runs) * kRun;
-            r.cnt = min(kRun, b.n[2] - r.k0);
+            r.cnt = has ? min(kRun, b.n[2] - r.k0) : 0;
             r.a0 = (((long long)(r.i + CNS_NG) * g1 + (r.j + CNS_NG)) * g2 + (r.k0 + CNS_NG)) * CNS_NC;
             for (int x = lane; x < r.cnt * CNS_NC; x += 32) sw[x] = h[r.a0 + x];
             __syncwarp();
-            if (GHOSTS) run_images(b, r, sw, h, lane);
+            if (GHOSTS && has) run_images(b, r, sw, h, lane);
             double cour = 0.0;
             int health = 0;
+            float est = -1.0f;
+            CourantInput64 cq;
             if (lane < r.cnt) {
                 const int k = r.k0 + lane;
                 const long long c = cell_off(b, r.i, r.j, k);
@@ -226,13 +229,28 @@ __global__ void __launch_bounds__(kWarps * 32) k_upload_deriv(BoxView b, double*
                     un[l] = sw[lane * CNS_NC + l];
                     b.U[c + l * b.fs] = un[l];
                 }
-                cour = epilogue<double>(b, (double*)b.P[b.sc->pbase], c, r.i, r.j, k, un, true, &health);
+                epilogue_plain(b, (double*)b.P[b.sc->pbase], c, r.i, r.j, k, un, &health, &cq);
+                est = courant_plain_est(b, cq);
             }
-            if (health) atomicOr(&b.sc->status, health);
-            courant_fold(b, cour);
-            __threadfence();  // this lane's stores, before the run is counted
-            __syncwarp();
-            if (lane == 0) atomicAdd(&done[r.i], 1);
+            // The Courant maximum through FP32 candidates over the item's 8 runs, as in stage 3
+            // of k_assemble: the FP64 number only where it can be the largest, bit for bit.
+            float m = est;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (lane == 0) s_max[warp] = m;
+            __syncthreads();
+            m = s_max[0];
+#pragma unroll
+            for (int w = 1; w < kWarps; w++) m = fmaxf(m, s_max[w]);
+            const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
+            if (lane < r.cnt && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f))) cour = courant_plain(b, cq);
+            if (has) {
+                if (health) atomicOr(&b.sc->status, health);
+                courant_fold(b, cour);
+                __threadfence();  // this lane's stores, before the run is counted
+                __syncwarp();
+                if (lane == 0) atomicAdd(&done[r.i], 1);
+            }
         } else {  // stage 1's derivative pass on tile ~item, once the planes it reads are in
             const Tile T = tiles[~item];
             int lo, hi;
