@@ -200,7 +200,8 @@ def cpu_baseline(n: int, seconds: float):
     from oracle import oracle as O
     O.build(ref=os.path.isdir(O.REF_SRC))
     cores = os.cpu_count() or 1
-    value, steps, wall = oracle_processes(n, 100, 1, seconds, cores)
+    nproc = host_processes(n)
+    value, steps, wall = oracle_processes(n, 100, 1, seconds, nproc)
     # one core, as the reference's own cpu/ path runs (its OpenMP pragmas are commented out)
     one = {}
     O.set_threads(1)
@@ -223,8 +224,8 @@ def cpu_baseline(n: int, seconds: float):
         e1 = time.perf_counter() - t1
         if e1 >= 4.0 or k >= 20:
             break
-    return {"value": value, "unit": "cell-updates/s", "cores": cores, "cpu_model": cpu_model(), "kind": "port",
-            "sample": f"{cores} single-threaded processes, {steps} RK3 steps in all of their own {n}^3 boxes, "
+    return {"value": value, "unit": "cell-updates/s", "cores": nproc, "cpu_model": cpu_model(), "kind": "port",
+            "sample": f"{nproc} single-threaded processes, {steps} RK3 steps in all of their own {n}^3 boxes, "
                       f"{wall:.1f} s", "one_core_by_n": one,
             "openmp_one_process": {"value": n ** 3 * k / e1, "threads": threads, "steps": k}}
 
@@ -248,6 +249,18 @@ def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
         if time.time() - t0 >= seconds:
             break
     out.put((k, t0, time.time()))
+
+
+def host_processes(n: int) -> int:
+    """Processes for oracle_processes: one per host core, but no more than a quarter of the
+    host's memory holds (an n^3 oracle step needs about 25 doubles per ghost-inclusive cell)."""
+    cores = os.cpu_count() or 1
+    try:
+        mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError, AttributeError):
+        return cores
+    per = 25 * 8 * (n + 8) ** 3
+    return max(1, min(cores, int(mem // 4 // per)))
 
 
 def oracle_processes(n, steps, warmup, seconds, nproc, which="port"):
@@ -304,11 +317,11 @@ def run_cpu_table(args):
         t0 = time.perf_counter()
         O.advance(U, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
         threads[str(n)] = n ** 3 * steps / (time.perf_counter() - t0)
-    agg, done, wall = oracle_processes(128, 3, 0, 1e9, cores)
+    agg, done, wall = oracle_processes(128, 3, 0, 1e9, host_processes(128))
     return {"workload": "CPU baseline: the oracle port of the reference's cpu/ path, sinusoidal field with a 1e-3 "
                         "perturbation (seed 1)", "unit": "cell-updates/s", "cores": cores, "cpu_model": cpu_model(),
             "one_core_by_n": one, "openmp_all_cores_by_n": threads,
-            "processes_128": {"processes": cores, "steps_each": 3, "aggregate": agg, "wall_s": wall}}
+            "processes_128": {"processes": host_processes(128), "steps_each": 3, "aggregate": agg, "wall_s": wall}}
 
 
 def run_reference(args, dist):
@@ -324,8 +337,8 @@ def run_reference(args, dist):
     O.build(ref=os.path.isdir(O.REF_SRC))
     use_ref = O.have_ref() and os.path.isdir(O.REF_SRC)
     which = "ref" if use_ref else "port"
-    cores = os.cpu_count() or 1
     n = args.n
+    cores = host_processes(n)
     warm = min(args.warmup, 1)
     v, done, wall = oracle_processes(n, args.steps, warm, 60.0, cores, which=which)
     steps = max(1, done // cores)
