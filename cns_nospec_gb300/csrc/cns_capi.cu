@@ -1074,7 +1074,7 @@ static int upload_first_step(cns_box* b, double* h_map, bool ghosts) {
     if (!b->d_counters) CK(cudaMalloc((void**)&b->d_counters, sizeof(int) * (b->desc.n[0] + 1)));
     CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
     CK(host_upload_deriv(b->view, h_map, ghosts, b->d_tiles, b->d_queue, b->nq, b->d_counters, b->stream));
-    CK(launch_refs(b->d_view, 1, b->stream));
+    // (no k_refs: the FP64 form does not use the mixed form's reference values)
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return enqueue_step(b->d_view, 1, box_lists(b), b->stream, nullptr, nullptr, true);
