@@ -468,7 +468,7 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
     if (health) atomicOr(&b.sc->status, health);
     if (STAGE == 3) {
         // The FP64 Courant number only of the cells that can hold this thread's maximum: with
-        // |est - exact| <= eps * exact (eps = 2^-20, 16x the estimate's error bound), a cell
+        // |est - exact| <= eps * exact (eps = 2^-20, over twice the estimate's ~7 * 2^-24), a cell
         // whose estimate is below (1 - 2 eps) of the largest estimate is below that cell's exact
         // value, so the maximum over the candidates is the maximum over all cells, bit for bit.
         // NaN or tiny estimates (outside the bound's range) are always candidates, and all cells
