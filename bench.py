@@ -52,8 +52,8 @@ def parse():
     p.add_argument("--case", choices=["fp64", "mixed", "e2e"], default=None,
                    help="profiling case: only upload + warmup + steps of one form (for ncu), then exit; "
                         "e2e: warmup + steps calls of cns_new_advance on a page-locked host array")
-    p.add_argument("--mixed-kernel", choices=["ws", "tma", "direct"], default=None,
-                   help="--case mixed: the assembly kernel (default: the library's choice, ws)")
+    p.add_argument("--kernel", choices=["ws", "tma", "direct"], default=None,
+                   help="--case: the assembly kernel (default: the library's choice; ws is mixed-only)")
     p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve", "cpu"], default="box",
                    help="box: the headline 128^3 line (default); batch: 256 uneven boxes; "
                         "mixed256: FP64 vs mixed at --size (use 256); serve: the request stream; "
@@ -522,9 +522,8 @@ def run_case(args):
         return
     prec = C.CNS_FP64 if args.case == "fp64" else C.CNS_MIXED
     box = C.Box(args.n, I.box_dx(args.n), I.CFL, I.ETA, I.ALAM, precision=prec)
-    if prec == C.CNS_MIXED and args.mixed_kernel:
-        box.set_kernel({"ws": C.CNS_ASSEMBLE_TMA_WS, "tma": C.CNS_ASSEMBLE_TMA,
-                        "direct": C.CNS_ASSEMBLE_DIRECT}[args.mixed_kernel])
+    if args.kernel:
+        box.set_kernel({"ws": C.CNS_ASSEMBLE_TMA_WS, "tma": C.CNS_ASSEMBLE_TMA, "direct": C.CNS_ASSEMBLE_DIRECT}[args.kernel])
     box.init_field(perturb=1e-3, seed=1)
     box.advance_timed(args.warmup)
     ms, launches, total = box.advance_timed(args.steps)

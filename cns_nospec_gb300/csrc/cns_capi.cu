@@ -174,7 +174,7 @@ static Geometry geometry(const cns_box_desc* d) {
     tma_tile_shape(&xi, &xj, &xk);
     g.nxtiles = 0;
     g.off_xtiles = g.off_maps = 0;
-    if (d->precision == CNS_MIXED) {
+    {  // the TMA assemblies' tiles and tensor maps (both forms)
         g.nxtiles = ((d->n[0] + xi - 1) / xi) * ((d->n[1] + xj - 1) / xj) * ((d->n[2] + xk - 1) / xk);
         g.off_xtiles = o;  o = align256(o + sizeof(Tile) * g.nxtiles);
         g.off_maps = o;    o = align256(o + tma_maps_bytes());
@@ -311,8 +311,8 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     b->ntiles = (int)tiles.size();
     std::vector<Tile> xtiles;
     std::vector<unsigned char> maps;
-    if (desc->precision == CNS_MIXED) {
-        // the TMA assembly needs the box's tensor maps; without a driver entry point for them
+    {
+        // the TMA assemblies need the box's tensor maps; without a driver entry point for them
         // the box stays on the direct kernel
         b->d_xtiles = (Tile*)(b->arena + g.off_xtiles);
         append_xtiles(desc->n, 0, xtiles);
@@ -320,7 +320,7 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
         maps.resize(tma_maps_bytes());
         if (tma_encode_maps(v, maps.data()) == cudaSuccess) {
             v.tma = b->arena + g.off_maps;
-            b->kernel = assemble_ws_fits() ? CNS_ASSEMBLE_TMA_WS : CNS_ASSEMBLE_TMA;
+            if (desc->precision == CNS_MIXED) b->kernel = assemble_ws_fits() ? CNS_ASSEMBLE_TMA_WS : CNS_ASSEMBLE_TMA;
         }
     }
     e = cudaMemsetAsync(b->arena, 0, g.total, b->stream);
@@ -483,8 +483,12 @@ extern "C" int cns_box_download(cns_box* b, double* U_host) {
 // The tiles of one RK3 step, split by kernel: FP64 boxes, mixed boxes (their derivative pass
 // always, their assembly when on the direct kernel), and mixed boxes on the TMA assembly.
 struct WorkLists {
-    const Tile* d64 = nullptr;
+    const Tile* d64 = nullptr;  // the derivative pass of FP64 boxes
     int nd64 = 0;
+    const Tile* a64 = nullptr;  // FP64 boxes on the direct assembly
+    int na64 = 0;
+    const Tile* x64 = nullptr;  // FP64 boxes on the TMA assembly
+    int nx64 = 0;
     const Tile* d32 = nullptr;
     int nd32 = 0;
     const Tile* a32 = nullptr;
@@ -526,8 +530,12 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
             CK(launch_deriv_tma(views, w.dx32, w.ndx32, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
-        if (w.nd64) {
-            CK(launch_assemble(0, views, w.d64, w.nd64, stage, st));
+        if (w.na64) {
+            CK(launch_assemble(0, views, w.a64, w.na64, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
+        if (w.nx64) {
+            CK(launch_assemble_tma64(views, w.x64, w.nx64, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
         if (w.na32) {
@@ -558,6 +566,10 @@ static WorkLists box_lists(const cns_box* b) {
             w.d32 = w.a32 = b->d_tiles, w.nd32 = w.na32 = b->ntiles;
     } else {
         w.d64 = b->d_tiles, w.nd64 = b->ntiles;
+        if (b->kernel == CNS_ASSEMBLE_TMA)
+            w.x64 = b->d_xtiles, w.nx64 = b->nxtiles;
+        else
+            w.a64 = b->d_tiles, w.na64 = b->ntiles;
     }
     return w;
 }
@@ -798,7 +810,7 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     WorkLists& w = bt->lists;
     w = WorkLists();
     Tile* at = bt->d_tiles;
-    w.d64 = at, w.nd64 = (int)d64.size(), at += d64.size();
+    w.d64 = w.a64 = at, w.nd64 = w.na64 = (int)d64.size(), at += d64.size();  // FP64: direct assembly
     w.d32 = at, w.nd32 = (int)d32.size(), at += d32.size();
     w.a32 = at, w.na32 = (int)a32.size(), at += a32.size();
     w.x32 = at, w.nx32 = (int)x32.size(), at += x32.size();
@@ -1319,8 +1331,10 @@ static int restore_state(cns_box* b, const BoxScalars* hs) {
 static int apply_kernel(cns_box* b, int kernel) {
     if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA && kernel != CNS_ASSEMBLE_TMA_WS)
         return fail(CNS_ERR_INVALID, "unknown kernel %d", kernel);
-    if (kernel != CNS_ASSEMBLE_DIRECT && (b->desc.precision != CNS_MIXED || !b->view.tma))
-        return fail(CNS_ERR_INVALID, "the TMA assemblies serve mixed-precision boxes with tensor maps only");
+    if (kernel != CNS_ASSEMBLE_DIRECT && !b->view.tma)
+        return fail(CNS_ERR_INVALID, "the TMA assemblies need the box's tensor maps");
+    if (kernel == CNS_ASSEMBLE_TMA_WS && b->desc.precision != CNS_MIXED)
+        return fail(CNS_ERR_INVALID, "the warp-specialised TMA assembly serves mixed-precision boxes only");
     if (kernel == b->kernel) return CNS_OK;
     CK(cudaStreamSynchronize(b->stream));
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
@@ -1354,6 +1368,8 @@ extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], in
     BoxScalars hs;
     int rc = save_state(b, &hs);
     if (rc) return rc;
+    // mixed boxes: the three assemblies; FP64 boxes: the direct one only (their TMA assembly,
+    // one block per SM, measured 23 % slower on GB300, is an explicit option)
     const int nkern = (b->desc.precision == CNS_MIXED && b->view.tma) ? 3 : 1;
     int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]}, best_k = b->kernel;
     double best_t = 1e300;

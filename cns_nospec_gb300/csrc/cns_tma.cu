@@ -83,7 +83,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
         if (global_ns() - t0 > 1000000000ull) return false;
     return true;
 }
-__device__ __forceinline__ void tma_load(float* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
                                          uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
@@ -92,9 +92,11 @@ __device__ __forceinline__ void tma_load(float* dst, const CUtensorMap* map, int
         : "memory");
 }
 
-// Issue the copy of `L` for tile `tile` into `buf`, completing on `bar`.
+// Issue the copy of `L` for tile `tile` into `buf`, completing on `bar` (R: float for mixed
+// boxes, double for FP64 boxes, whose tensor maps are FP64).
+template <class R>
 __device__ __forceinline__ void issue_load(const BoxView* boxes, const Tile* tiles, int tile, const Load L, int flip,
-                                           float* buf, uint64_t* bar) {
+                                           R* buf, uint64_t* bar) {
     const Tile T = tiles[tile];
     const BoxView& b = boxes[T.box];
     const TmaMaps* maps = (const TmaMaps*)b.tma;
@@ -106,12 +108,13 @@ __device__ __forceinline__ void issue_load(const BoxView* boxes, const Tile* til
         map = &maps->s[si];
     }
     const int hk = box_k(L.shape) == XK ? 0 : 4, hj = box_j(L.shape) == XJ ? 0 : 4, hi = box_i(L.shape) == XI ? 0 : 4;
-    mbar_expect_tx(bar, (uint32_t)(box_elems(L.shape) * sizeof(float)));
+    mbar_expect_tx(bar, (uint32_t)(box_elems(L.shape) * sizeof(R)));
     tma_load(buf, map, T.k0 + CNS_NG - hk, T.j0 + CNS_NG - hj, T.i0 + CNS_NG - hi, L.field, bar);
 }
 // Load number g of this block in kSched (tile g / 20, entry g % 20).
+template <class R>
 __device__ __forceinline__ void issue(const BoxView* boxes, const Tile* tiles, int tile, int entry, int flip,
-                                      float* buf, uint64_t* bar) {
+                                      R* buf, uint64_t* bar) {
     issue_load(boxes, tiles, tile, kSched[entry], flip, buf, bar);
 }
 
@@ -142,64 +145,71 @@ __device__ __forceinline__ void prefetch_state_l2(const BoxView& b, const Tile& 
     }
 }
 
-__device__ __forceinline__ float sd1acc(float acc, const float* p, int s, const float* a) {
-    acc = fmaf(a[0], p[s] - p[-s], acc);
-    acc = fmaf(a[1], p[2 * s] - p[-2 * s], acc);
-    acc = fmaf(a[2], p[3 * s] - p[-3 * s], acc);
-    acc = fmaf(a[3], p[4 * s] - p[-4 * s], acc);
+template <class R>
+__device__ __forceinline__ R sd1acc(R acc, const R* p, int s, const R* a) {
+    acc = fma(a[0], p[s] - p[-s], acc);
+    acc = fma(a[1], p[2 * s] - p[-2 * s], acc);
+    acc = fma(a[2], p[3 * s] - p[-3 * s], acc);
+    acc = fma(a[3], p[4 * s] - p[-4 * s], acc);
     return acc;
 }
-__device__ __forceinline__ float sd1(const float* p, int s, const float* a) {
-    float acc = a[0] * (p[s] - p[-s]);
-    acc = fmaf(a[1], p[2 * s] - p[-2 * s], acc);
-    acc = fmaf(a[2], p[3 * s] - p[-3 * s], acc);
-    acc = fmaf(a[3], p[4 * s] - p[-4 * s], acc);
+template <class R>
+__device__ __forceinline__ R sd1(const R* p, int s, const R* a) {
+    R acc = a[0] * (p[s] - p[-s]);
+    acc = fma(a[1], p[2 * s] - p[-2 * s], acc);
+    acc = fma(a[2], p[3 * s] - p[-3 * s], acc);
+    acc = fma(a[3], p[4 * s] - p[-4 * s], acc);
     return acc;
 }
-__device__ __forceinline__ float sd2acc(float acc, const float* p, int s, const float* b) {
-    acc = fmaf(b[0], p[s] + p[-s], acc);
-    acc = fmaf(b[1], p[2 * s] + p[-2 * s], acc);
-    acc = fmaf(b[2], p[3 * s] + p[-3 * s], acc);
-    acc = fmaf(b[3], p[4 * s] + p[-4 * s], acc);
+template <class R>
+__device__ __forceinline__ R sd2acc(R acc, const R* p, int s, const R* b) {
+    acc = fma(b[0], p[s] + p[-s], acc);
+    acc = fma(b[1], p[2 * s] + p[-2 * s], acc);
+    acc = fma(b[2], p[3 * s] + p[-3 * s], acc);
+    acc = fma(b[3], p[4 * s] + p[-4 * s], acc);
     return acc;
 }
 // the same on a register column (i direction), centre index c
-__device__ __forceinline__ float cd1acc(float acc, const float* col, int c, const float* a) {
-    acc = fmaf(a[0], col[c + 1] - col[c - 1], acc);
-    acc = fmaf(a[1], col[c + 2] - col[c - 2], acc);
-    acc = fmaf(a[2], col[c + 3] - col[c - 3], acc);
-    acc = fmaf(a[3], col[c + 4] - col[c - 4], acc);
+template <class R>
+__device__ __forceinline__ R cd1acc(R acc, const R* col, int c, const R* a) {
+    acc = fma(a[0], col[c + 1] - col[c - 1], acc);
+    acc = fma(a[1], col[c + 2] - col[c - 2], acc);
+    acc = fma(a[2], col[c + 3] - col[c - 3], acc);
+    acc = fma(a[3], col[c + 4] - col[c - 4], acc);
     return acc;
 }
-__device__ __forceinline__ float cd1(const float* col, int c, const float* a) {
-    float acc = a[0] * (col[c + 1] - col[c - 1]);
-    acc = fmaf(a[1], col[c + 2] - col[c - 2], acc);
-    acc = fmaf(a[2], col[c + 3] - col[c - 3], acc);
-    acc = fmaf(a[3], col[c + 4] - col[c - 4], acc);
+template <class R>
+__device__ __forceinline__ R cd1(const R* col, int c, const R* a) {
+    R acc = a[0] * (col[c + 1] - col[c - 1]);
+    acc = fma(a[1], col[c + 2] - col[c - 2], acc);
+    acc = fma(a[2], col[c + 3] - col[c - 3], acc);
+    acc = fma(a[3], col[c + 4] - col[c - 4], acc);
     return acc;
 }
-__device__ __forceinline__ float cd2acc(float acc, const float* col, int c, const float* b) {
-    acc = fmaf(b[0], col[c + 1] + col[c - 1], acc);
-    acc = fmaf(b[1], col[c + 2] + col[c - 2], acc);
-    acc = fmaf(b[2], col[c + 3] + col[c - 3], acc);
-    acc = fmaf(b[3], col[c + 4] + col[c - 4], acc);
+template <class R>
+__device__ __forceinline__ R cd2acc(R acc, const R* col, int c, const R* b) {
+    acc = fma(b[0], col[c + 1] + col[c - 1], acc);
+    acc = fma(b[1], col[c + 2] + col[c - 2], acc);
+    acc = fma(b[2], col[c + 3] + col[c - 3], acc);
+    acc = fma(b[3], col[c + 4] + col[c - 4], acc);
     return acc;
 }
 
 // The full-box (u, v, w or T) pass: centre weight, then the i, j, k second differences.
-__device__ __forceinline__ void lap_full(const float* s, int tj, int tk, float cw, const float* wi, const float* wj,
-                                         const float* wk, float* acc, float* ctr, bool init_from_acc) {
+template <class R>
+__device__ __forceinline__ void lap_full(const R* s, int tj, int tk, R cw, const R* wi, const R* wj, const R* wk,
+                                         R* acc, R* ctr, bool init_from_acc) {
     using B = Bx<BX_FULL>;
-    float col[16];
+    R col[16];
 #pragma unroll
     for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk + 4)];
 #pragma unroll
     for (int i = 0; i < XI; i++) {
-        const float c0 = col[i + 4];
+        const R c0 = col[i + 4];
         ctr[i] = c0;
-        float a = init_from_acc ? fmaf(cw, c0, acc[i]) : cw * c0;
+        R a = init_from_acc ? fma(cw, c0, acc[i]) : cw * c0;
         a = cd2acc(a, col, i + 4, wi);
-        const float* p = s + B::at(i + 4, tj + 4, tk + 4);
+        const R* p = s + B::at(i + 4, tj + 4, tk + 4);
         a = sd2acc(a, p, B::K, wj);
         a = sd2acc(a, p, 1, wk);
         acc[i] = a;
@@ -210,9 +220,9 @@ __device__ __forceinline__ void lap_full(const float* s, int tj, int tk, float c
 // variables (f1..f4 accumulate in dmx, dmy, dmz, de) and the centre velocity c0.
 
 // Field e of a tile's 20 loads (schedule kSched), staged at s, folded into the sums.
-__device__ __forceinline__ void consume_field(int e, const float* s, const Tile& T, const BoxView& b,
-                                              const CoefT<float>& cf, int tj, int tk, float* dmx, float* dmy,
-                                              float* dmz, float* de, float* f0, float* c0) {
+template <class R>
+__device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, const BoxView& b, const CoefT<R>& cf,
+                                              int tj, int tk, R* dmx, R* dmy, R* dmz, R* de, R* f0, R* c0) {
     switch (e) {
         case 0: {  // SPHI: de starts from eta * Phi
             using B = Bx<BX_C>;
@@ -221,7 +231,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
             break;
         }
         case 1: {  // PT: de = tc T0 + phi, then the x, y, z second differences
-            float t0[XI];
+            R t0[XI];
             lap_full(s, tj, tk, cf.tc, cf.tl[0], cf.tl[1], cf.tl[2], de, t0, true);
             break;
         }
@@ -230,13 +240,13 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
             break;
         case 3: {  // SX: dmx += (eta/3) d/dx (v_y + w_z); then the work term dmx u0
             using B = Bx<BX_I>;
-            float col[16];
+            R col[16];
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
             for (int i = 0; i < XI; i++) {
                 dmx[i] = cd1acc(dmx[i], col, i + 4, cf.mx[0]);
-                de[i] = fmaf(dmx[i], c0[i], de[i]);
+                de[i] = fma(dmx[i], c0[i], de[i]);
             }
             break;
         }
@@ -248,7 +258,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
 #pragma unroll
             for (int i = 0; i < XI; i++) {
                 dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
-                de[i] = fmaf(dmy[i], c0[i], de[i]);
+                de[i] = fma(dmy[i], c0[i], de[i]);
             }
             break;
         }
@@ -260,13 +270,13 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
 #pragma unroll
             for (int i = 0; i < XI; i++) {
                 dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.mx[2]);
-                de[i] = fmaf(dmz[i], c0[i], de[i]);
+                de[i] = fma(dmz[i], c0[i], de[i]);
             }
             break;
         }
         case 8: {  // PMX: f0 = -d(rho u)/dx
             using B = Bx<BX_I>;
-            float col[16];
+            R col[16];
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
@@ -287,7 +297,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
         }
         case 11: {  // PFUU along x -> f1 (in dmx)
             using B = Bx<BX_I>;
-            float col[16];
+            R col[16];
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
@@ -296,7 +306,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
         }
         case 12: {  // PFUV: along y -> f1, along x -> f2 (in dmy)
             using B = Bx<BX_IJ>;
-            float col[16];
+            R col[16];
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk)];
 #pragma unroll
@@ -308,7 +318,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
         }
         case 13: {  // PFUW: along z -> f1, along x -> f3 (in dmz)
             using B = Bx<BX_IK>;
-            float col[16];
+            R col[16];
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk + 4)];
 #pragma unroll
@@ -328,7 +338,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
             using B = Bx<BX_JK>;
 #pragma unroll
             for (int i = 0; i < XI; i++) {
-                const float* p = s + B::at(i, tj + 4, tk + 4);
+                const R* p = s + B::at(i, tj + 4, tk + 4);
                 dmy[i] = sd1acc(dmy[i], p, 1, cf.ha[2]);
                 dmz[i] = sd1acc(dmz[i], p, B::K, cf.ha[1]);
             }
@@ -342,7 +352,7 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
         }
         case 17: {  // PHU along x -> f4 (in de)
             using B = Bx<BX_I>;
-            float col[16];
+            R col[16];
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
@@ -355,18 +365,24 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
             for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
             break;
         }
-        default: {  // 19, PHW; then -H_ref div(u) (the P set holds ((E+p) - H_ref) u), with
-                   // div(u) = (S_x + S_y + S_z) / 2 read at the cell (S is L2-resident)
+        default: {  // 19, PHW; for mixed boxes then -H_ref div(u) (their P set holds
+                   // ((E+p) - H_ref) u), with div(u) = (S_x + S_y + S_z) / 2 read at the cell (S is
+                   // L2-resident)
             using B = Bx<BX_K>;
-            const float href = -(float)b.sc->H_ref;
-            const float* S = (const float*)b.S;
-            const int j = min(T.j0 + tj, b.n[1] - 1), k = min(T.k0 + tk, b.n[2] - 1);
+            if constexpr (sizeof(R) == 4) {
+                const float href = -(float)b.sc->H_ref;
+                const float* S = (const float*)b.S;
+                const int j = min(T.j0 + tj, b.n[1] - 1), k = min(T.k0 + tk, b.n[2] - 1);
 #pragma unroll
-            for (int i = 0; i < XI; i++) {
-                const long long c = cell_off(b, min(T.i0 + i, b.n[0] - 1), j, k);
-                const float hsum = __ldg(S + SX * b.fs + c) + __ldg(S + SY * b.fs + c) + __ldg(S + SZ * b.fs + c);
-                const float a = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
-                de[i] = fmaf(href, 0.5f * hsum, a);
+                for (int i = 0; i < XI; i++) {
+                    const long long c = cell_off(b, min(T.i0 + i, b.n[0] - 1), j, k);
+                    const float hsum = __ldg(S + SX * b.fs + c) + __ldg(S + SY * b.fs + c) + __ldg(S + SZ * b.fs + c);
+                    const float a = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                    de[i] = fmaf(href, 0.5f * hsum, a);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
             }
             break;
         }
@@ -375,8 +391,9 @@ __device__ __forceinline__ void consume_field(int e, const float* s, const Tile&
 
 // Park the five sums of a thread's 8 cells at column `col` of a 40 KB stash; the write-back
 // reads them back as stash[(i * 5 + l) * 256 + col].
-__device__ __forceinline__ void park_sums(float* stash, int col, const float* f0, const float* dmx, const float* dmy,
-                                          const float* dmz, const float* de) {
+template <class R>
+__device__ __forceinline__ void park_sums(R* stash, int col, const R* f0, const R* dmx, const R* dmy, const R* dmz,
+                                          const R* de) {
 #pragma unroll
     for (int i = 0; i < XI; i++) {
         stash[(i * 5 + 0) * kTileThreads + col] = f0[i];
@@ -498,12 +515,94 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
     }
 }
 
+// The FP64 box's write-back of the 8 cells of column `col` = (tj, tk) of tile T from the FP64
+// sums parked in `stash`: the RK3 combine, the host array (stage 3), ctoprim and fluxes as in
+// k_assemble<double> (same operations, same bits), and at stage 3 the Courant maximum through
+// FP32 candidates over the whole tile (each cell's estimate and p parked over its sums, a block
+// maximum, the FP64 number only where it can be the largest).  All threads of the block take
+// part (block barriers at stage 3).
 template <int STAGE>
-__global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView* __restrict__ boxes,
-                                                               const Tile* __restrict__ tiles, int ntiles) {
+__device__ __forceinline__ void write_back_plain(const BoxView& b, const Tile& T, double* stash, int col, int tj,
+                                                 int tk) {
+    const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
+    double* Pw = (double*)b.P[pr ^ 1];
+    const double dt = b.sc->dt;
+    const int j = T.j0 + tj, k = T.k0 + tk;
+    const long long fs = b.fs;
+    float m32 = -1.0f;
+    int health = 0;
+#pragma unroll 1
+    for (int i = 0; i < XI; i++) {
+        const int ic = T.i0 + i;
+        if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+        const long long c = cell_off(b, ic, j, k);
+        double un[5];
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+            const long long e = c + l * fs;
+            const double r = stash[(i * 5 + l) * kTileThreads + col];
+            if (STAGE == 1) {
+                un[l] = fma(dt, r, b.U[e]);
+                b.Us[e] = un[l];
+            } else if (STAGE == 2) {
+                un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                b.Us[e] = un[l];
+            } else {
+                un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
+                b.U[e] = un[l];
+            }
+        }
+        if (STAGE == 3 && b.host_out) store_host(b, ic, j, k, un);
+        CourantInput64 q;
+        epilogue_plain(b, Pw, c, ic, j, k, un, &health, &q);
+        if (STAGE == 3) {
+            const float est = courant_plain_est(b, q);
+            reinterpret_cast<float*>(stash + (i * 5 + 0) * kTileThreads + col)[0] = est;
+            stash[(i * 5 + 1) * kTileThreads + col] = q.p;
+            m32 = fmaxf(m32, est);
+        }
+    }
+    if (health) atomicOr(&b.sc->status, health);
+    if (STAGE == 3) {
+        __shared__ float s_max[kTileThreads / 32];
+        float m = m32;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+        __syncthreads();
+        m = s_max[0];
+#pragma unroll
+        for (int w = 1; w < kTileThreads / 32; w++) m = fmaxf(m, s_max[w]);
+        __syncthreads();  // s_max is rewritten for the next tile
+        const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
+        double cmax = 0.0;
+#pragma unroll 1
+        for (int i = 0; i < XI; i++) {
+            const int ic = T.i0 + i;
+            if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+            const float est = reinterpret_cast<const float*>(stash + (i * 5 + 0) * kTileThreads + col)[0];
+            if (m <= 3.0e38f && est < thr && est > 1e-30f) continue;
+            // the cell's Courant number from its new state, as epilogue_plain formed it
+            const long long c = cell_off(b, ic, j, k);
+            const double rho = b.U[c], rinv = rcp_nr(rho);
+            const CourantInput64 q{stash[(i * 5 + 1) * kTileThreads + col], rinv, b.U[c + fs] * rinv,
+                                   b.U[c + 2 * fs] * rinv, b.U[c + 3 * fs] * rinv};
+            const double cour = courant_plain(b, q);
+            cmax = cour > cmax ? cour : cmax;
+        }
+        courant_fold(b, cmax);
+    }
+}
+
+// R = float: mixed boxes, two blocks per SM (80 KB of shared memory each); R = double: FP64
+// boxes, one block per SM (160 KB), with up to 255 registers for the 8 cells' FP64 sums.
+template <class R, int STAGE>
+__global__ void __launch_bounds__(kTileThreads, sizeof(R) == 4 ? 2 : 1) k_assemble_tma(const BoxView* __restrict__ boxes,
+                                                                                   const Tile* __restrict__ tiles,
+                                                                                   int ntiles) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* buf[2] = {(float*)smem_raw, (float*)smem_raw + kBufElems};
-    uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(float));
+    R* buf[2] = {(R*)smem_raw, (R*)smem_raw + kBufElems};
+    uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(R));
     const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
     const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     if (my_tiles <= 0) return;
@@ -517,18 +616,18 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
     constexpr int flip = (STAGE - 1) & 1;
     if (tid == 0) issue(boxes, tiles, blockIdx.x, 0, flip, buf[0], &bar[0]);
 
-    float dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
+    R dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
     int g = 0;
     for (int it = 0; it < my_tiles; it++) {
         const int tile = blockIdx.x + it * gridDim.x;
         const Tile T = tiles[tile];
         const BoxView& b = boxes[T.box];
-        const CoefT<float>& cf = b.c32;
+        const CoefT<R>& cf = coefs<R>(b);
         prefetch_state_l2(b, T, STAGE, tid);
         // Every sum is first written, not accumulated, by its first load; clearing them here
         // only tells the compiler that the last tile's values are dead once they are parked.
 #pragma unroll
-        for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.f;
+        for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = R(0);
         for (int e = 0; e < kLoads; e++, g++) {
             if (tid == 0 && g + 1 < total) {
                 const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
@@ -550,9 +649,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble_tma(const BoxView*
         // The sums are parked in the buffer the last field used (free: every thread passed the
         // barrier after consuming it; each thread reads back only its own entries), so the
         // write-back runs as a rolled loop and its code exists once, not 8x.
-        float* stash = buf[(g - 1) & 1];
+        R* stash = buf[(g - 1) & 1];
         park_sums(stash, tid, f0, dmx, dmy, dmz, de);
-        write_back<STAGE>(b, T, stash, tid, tj, tk);
+        if constexpr (sizeof(R) == 4)
+            write_back<STAGE>(b, T, stash, tid, tj, tk);
+        else
+            write_back_plain<STAGE>(b, T, stash, tid, tj, tk);
         __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
     }
 }
@@ -815,12 +917,15 @@ cudaError_t tma_encode_maps(const BoxView& v, void* out) {
     if (!enc) return cudaErrorNotSupported;
     TmaMaps* m = (TmaMaps*)out;
     const cuuint64_t g0 = v.n[0] + 2 * CNS_NG, g1 = v.n[1] + 2 * CNS_NG, g2 = v.n[2] + 2 * CNS_NG;
+    const bool fp64 = v.precision == 0;  // FP64 boxes: P and S sets in double
+    const cuuint64_t es_bytes = fp64 ? 8 : 4;
     auto one = [&](CUtensorMap* map, void* base, int nfields, int shape) -> bool {
         const cuuint64_t dims[4] = {g2, g1, g0, (cuuint64_t)nfields};
-        const cuuint64_t strides[3] = {(cuuint64_t)v.sj * 4, (cuuint64_t)v.si * 4, (cuuint64_t)v.fs * 4};
+        const cuuint64_t strides[3] = {(cuuint64_t)v.sj * es_bytes, (cuuint64_t)v.si * es_bytes, (cuuint64_t)v.fs * es_bytes};
         const cuuint32_t box[4] = {(cuuint32_t)box_k(shape), (cuuint32_t)box_j(shape), (cuuint32_t)box_i(shape), 1};
         const cuuint32_t es[4] = {1, 1, 1, 1};
-        return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        return enc(map, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides,
+                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
     };
@@ -833,26 +938,35 @@ cudaError_t tma_encode_maps(const BoxView& v, void* out) {
     return cudaSuccess;
 }
 
-template <int STAGE>
+template <class R, int STAGE>
 static cudaError_t launch_tma_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
-    auto fn = k_assemble_tma<STAGE>;
-    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem);
+    auto fn = k_assemble_tma<R, STAGE>;
+    constexpr size_t smem = 2 * kBufElems * sizeof(R) + 2 * sizeof(uint64_t);
+    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kTileThreads, kTmaSmem);
-    if (per < 1) per = 1;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kTileThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
     const int grid = ntiles < nsm * per ? ntiles : nsm * per;
-    fn<<<grid, kTileThreads, kTmaSmem, st>>>(boxes, tiles, ntiles);
+    fn<<<grid, kTileThreads, smem, st>>>(boxes, tiles, ntiles);
     return cudaGetLastError();
 }
 
 cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (ntiles <= 0) return cudaSuccess;
-    if (stage == 1) return launch_tma_stage<1>(boxes, tiles, ntiles, st);
-    if (stage == 2) return launch_tma_stage<2>(boxes, tiles, ntiles, st);
-    return launch_tma_stage<3>(boxes, tiles, ntiles, st);
+    if (stage == 1) return launch_tma_stage<float, 1>(boxes, tiles, ntiles, st);
+    if (stage == 2) return launch_tma_stage<float, 2>(boxes, tiles, ntiles, st);
+    return launch_tma_stage<float, 3>(boxes, tiles, ntiles, st);
+}
+
+cudaError_t launch_assemble_tma64(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (stage == 1) return launch_tma_stage<double, 1>(boxes, tiles, ntiles, st);
+    if (stage == 2) return launch_tma_stage<double, 2>(boxes, tiles, ntiles, st);
+    return launch_tma_stage<double, 3>(boxes, tiles, ntiles, st);
 }
 
 template <class Fn>
