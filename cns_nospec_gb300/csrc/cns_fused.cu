@@ -171,7 +171,9 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
             for (int q = 1; q < kTileThreads / 32; q++) m = fmaxf(m, s_max[q]);
             __syncthreads();  // s_max is rewritten for the next tile
             const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
-            if (inside && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f))) cour = courant_plain(b, cq);
+            const float gcut = courant_running_max(b);
+            if (inside && !courant_below(est, gcut) && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f)))
+                cour = courant_plain(b, cq);
         }
         if (STAGE == 3) courant_fold(b, cour);
     }

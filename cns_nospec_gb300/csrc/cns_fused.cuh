@@ -203,6 +203,19 @@ __device__ __forceinline__ float f32_cut(double d) {
         return __uint_as_float((hi & 0x80000000u) | (((hi & 0x7FFFFFFFu) << 3) - 0xC0000000u));
     return __uint_as_float((((hi & 0x7FFFFFFFu) | lo) == 0u) ? (hi & 0x80000000u) : 0x7FC00000u);
 }
+// The box's running Courant maximum (the exact FP64 numbers folded in so far), cut to FP32 on
+// the integer pipes: a lower bound.  Read by lane 0 and broadcast; all lanes call it.
+__device__ __forceinline__ float courant_running_max(const BoxView& b) {
+    unsigned long long bits = 0;
+    if ((threadIdx.x & 31) == 0) bits = *(volatile const unsigned long long*)&b.sc->courno_bits;
+    return f32_cut(__longlong_as_double((long long)__shfl_sync(0xffffffffu, bits, 0)));
+}
+// A cell whose FP32 Courant estimate, widened by a bound on its error (2^-18, over the
+// estimates' ~1.4 * 2^-20), stays below that running maximum cannot be the maximum: its exact
+// number is below a value some cell already has.  Tiny or NaN estimates never pass this test.
+__device__ __forceinline__ bool courant_below(float est, float running) {
+    return est > 1e-30f && est * (1.0f + 0x1p-18f) < running;
+}
 // An FP32 estimate of courant_plain from those cut inputs: counting 2^-20 per cut input and
 // 2^-24 per FP32 rounding (1.4, two products, sqrt, the sum, 1/dx, the last product) it lies
 // within ~1.4 * 2^-20 of it (courant_eps is 2^-18) for states whose values are normal FP32

@@ -243,7 +243,9 @@ __global__ void __launch_bounds__(kWarps * 32) k_upload_deriv(BoxView b, double*
 #pragma unroll
             for (int w = 1; w < kWarps; w++) m = fmaxf(m, s_max[w]);
             const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
-            if (lane < r.cnt && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f))) cour = courant_plain(b, cq);
+            const float gcut = courant_running_max(b);
+            if (lane < r.cnt && !courant_below(est, gcut) && (!(m <= 3.0e38f) || !(est < thr) || !(est > 1e-30f)))
+                cour = courant_plain(b, cq);
             if (has) {
                 if (health) atomicOr(&b.sc->status, health);
                 courant_fold(b, cour);

@@ -491,14 +491,17 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
         // NaN or tiny estimates (outside the bound's range) are always candidates, and all cells
         // are when an estimate overflowed.  The warp runs the FP64 code once per round of
         // candidates (mostly one), not once per cell.
+        // Cells whose estimate, widened by its bound, stays below the box's running maximum
+        // (the exact FP64 numbers earlier tiles folded in) cannot be the maximum either.
         const float thr = m32 * (1.0f - 0x1p-18f);
         const bool all = !(m32 <= 3.0e38f);
+        const float gcut = courant_running_max(b);
         unsigned cand = 0;
 #pragma unroll
         for (int i = 0; i < XI; i++) {
             const float est = stash[(i * 5 + 0) * kTileThreads + col];
             const bool inside = T.i0 + i < b.n[0] && j < b.n[1] && k < b.n[2];
-            if (inside && (all || !(est < thr) || !(est > 1e-30f))) cand |= 1u << i;
+            if (inside && !courant_below(est, gcut) && (all || !(est < thr) || !(est > 1e-30f))) cand |= 1u << i;
         }
         while (__any_sync(0xffffffffu, cand != 0)) {
             if (cand) {
@@ -575,13 +578,14 @@ __device__ __forceinline__ void write_back_plain(const BoxView& b, const Tile& T
         for (int w = 1; w < kTileThreads / 32; w++) m = fmaxf(m, s_max[w]);
         __syncthreads();  // s_max is rewritten for the next tile
         const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
+        const float gcut = courant_running_max(b);
         double cmax = 0.0;
 #pragma unroll 1
         for (int i = 0; i < XI; i++) {
             const int ic = T.i0 + i;
             if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
             const float est = reinterpret_cast<const float*>(stash + (i * 5 + 0) * kTileThreads + col)[0];
-            if (m <= 3.0e38f && est < thr && est > 1e-30f) continue;
+            if ((m <= 3.0e38f && est < thr && est > 1e-30f) || courant_below(est, gcut)) continue;
             // the cell's Courant number from its new state, as epilogue_plain formed it
             const long long c = cell_off(b, ic, j, k);
             const double rho = b.U[c], rinv = rcp_nr(rho);
