@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(kTileThreads) k_prim(const BoxView* __restrict
 template <class R>
 __global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
                                                       int ntiles, int stage) {
+    pdl_enter();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
@@ -53,6 +54,7 @@ __global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restric
 template <class R, int STAGE>
 __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __restrict__ boxes,
                                                          const Tile* __restrict__ tiles, int ntiles) {
+    pdl_enter();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
@@ -198,6 +200,7 @@ __global__ void k_refs(const BoxView* __restrict__ boxes, int nboxes) {
 
 // ---- k_stepend: dt for the next step from the Courant max (cpu/advance.cpp:52-58) ----------
 __global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int flip) {
+    pdl_enter();
     const int bx = blockIdx.x * blockDim.x + threadIdx.x;
     if (bx >= nboxes) return;
     BoxScalars* s = boxes[bx].sc;
@@ -234,22 +237,20 @@ static cudaError_t launch_prim_t(const BoxView* boxes, const Tile* tiles, int nt
 template <class R>
 static cudaError_t launch_deriv_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     auto fn = k_deriv<R>;
-    fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles, stage);
-    return cudaGetLastError();
+    return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles, stage);
 }
 template <class R>
 static cudaError_t launch_assemble_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (stage == 1) {
         auto fn = k_assemble<R, 1>;
-        fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
+        return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else if (stage == 2) {
         auto fn = k_assemble<R, 2>;
-        fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
+        return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else {
         auto fn = k_assemble<R, 3>;
-        fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
+        return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
@@ -275,8 +276,7 @@ cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st) {
 }
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st) {
     if (nboxes <= 0) return cudaSuccess;
-    k_stepend<<<(nboxes + 127) / 128, 128, 0, st>>>(boxes, nboxes, flip);
-    return cudaGetLastError();
+    return launch_pdl(k_stepend, (nboxes + 127) / 128, 128, 0, st, boxes, nboxes, flip);
 }
 
 }  // namespace cns

@@ -7,6 +7,23 @@
 
 namespace cns {
 
+// Launch a step kernel with programmatic stream serialization (see pdl_enter): it may start
+// while the previous kernel of the stream drains, and waits for it on the device.
+template <class... Params, class... Args>
+cudaError_t launch_pdl(void (*fn)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+
 // record the calling thread's last error (read back by cns_last_error); returns `code`
 int set_error(int code, const char* msg);
 
