@@ -205,17 +205,19 @@ static void fill_coefs(BoxView& v, const cns_box_desc* d) {
     CoefT<double>& c = v.c64;
     memset(&c, 0, sizeof c);
     double tsum = 0.0;
+    // heat conduction alam lap(T) = (alam / c_v) lap(e): the P set carries e, not T
+    const double alam_cv = d->alam * (1.0 / kCv);
     for (int a = 0; a < 3; a++) {
         for (int m = 0; m < 4; m++) {
             c.da[a][m] = A[m] * dxi[a];
             c.ha[a][m] = -A[m] * dxi[a];
             c.mx[a][m] = (d->eta * (1.0 / 3.0)) * A[m] * dxi[a];
-            c.tl[a][m] = d->alam * B[m] * (dxi[a] * dxi[a]);
+            c.tl[a][m] = alam_cv * B[m] * (dxi[a] * dxi[a]);
         }
         tsum += dxi[a] * dxi[a];
         c.cour[a] = dxi[a];
     }
-    c.tc = d->alam * kCenter * tsum;
+    c.tc = alam_cv * kCenter * tsum;
     for (int comp = 0; comp < 3; comp++) {
         double sum = 0.0;
         for (int a = 0; a < 3; a++) {

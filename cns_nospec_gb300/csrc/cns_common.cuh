@@ -31,7 +31,8 @@ enum { URHO = 0, UMX, UMY, UMZ, UENE };
 // cell by the epilogue of the previous stage (ctoprim fused there) with its periodic ghost
 // images, so no stencil ever recomputes a neighbour's primitive.
 enum {
-    PU = 0, PV, PW, PT,        // velocities and temperature (diffterm)
+    PU = 0, PV, PW, PT,        // velocities, and c_v T = e for the heat conduction (diffterm; its
+                               // coefficients carry alam / c_v, so T itself is never formed)
     PMX, PMY, PMZ,             // rho u, rho v, rho w  (density flux)
     PFUU, PFVV, PFWW,          // rho u u + p, rho v v + p, rho w w + p
     PFUV, PFUW, PFVW,          // rho u v, rho u w, rho v w
@@ -54,8 +55,8 @@ struct CoefT {
     R mx[3][4];     // mixed viscous term: (eta/3) a_m / dx_d
     R vl[3][3][4];  // viscous Laplacian of velocity c along d: eta (4/3 if c==d) b_m / dx_d^2
     R vc[3];        // its centre weight: eta c0 sum_d (4/3 if c==d) / dx_d^2
-    R tl[3][4];     // heat conduction along d: alam b_m / dx_d^2
-    R tc;           // alam c0 sum_d 1/dx_d^2
+    R tl[3][4];     // heat conduction along d: (alam / c_v) b_m / dx_d^2, applied to e = c_v T
+    R tc;           // (alam / c_v) c0 sum_d 1/dx_d^2
     R cour[3];      // 1/dx_d (Courant number)
     R eta;          // viscosity
 };
@@ -70,7 +71,7 @@ struct BoxScalars {
     int status;                      // HEALTH_* bits, sticky
     int pad;
     // Reference values of the mixed form, fixed at upload from one cell of the state (FP64):
-    // the FP32 stencil fields carry p - p_ref, T - T_ref and (E + p) - H_ref, whose rounding
+    // the FP32 stencil fields carry p - p_ref, e - e_ref and (E + p) - H_ref, whose rounding
     // is ~10-30x smaller than that of p, T, E + p themselves.  Every difference operator
     // annihilates a constant, and the energy flux splits exactly as
     // d((E+p) u)/dx = H_ref du/dx + d(((E+p) - H_ref) u)/dx.

@@ -177,7 +177,8 @@ __device__ __forceinline__ int health_bits(double rho, double eint) {
 // with the periodic face images each field's stencils need.  Returns the cell's Courant
 // number (only formed when `want_cour`).  Plain form: everything in FP64 (reciprocal by
 // rcp_nr).  Mixed form: E/rho, the subtraction e = E/rho - |u|^2/2 and the offsets
-// p - p_ref, T - T_ref, E - E_ref in FP64; the rest in FP32 (see BoxScalars).
+// p - p_ref, e - e_ref, E - E_ref in FP64; the rest in FP32 (see BoxScalars).  Both store e
+// (= c_v T) for the heat conduction, whose coefficients carry 1 / c_v.
 template <class R>
 __device__ __forceinline__ double epilogue(const BoxView& b, R* __restrict__ Pw, long long c, int i, int j, int k,
                                            const double un[5], bool want_cour, int* health);
@@ -248,7 +249,6 @@ __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restr
     const double ke = fma(u, u, fma(v, v, w * w));
     const double eint = fma(-0.5, ke, E * rinv);
     const double p = (kGm1 * eint) * rho;
-    const double T = eint * (1.0 / kCv);
     const double H = E + p;
     *health |= health_bits(rho, eint);
     // Field by field, not store_pset: its 16 live FP64 values would cost the upload kernels
@@ -256,7 +256,7 @@ __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restr
     store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
     store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
     store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
-    store_img(Pw + PT * fs, b, c, i, j, k, T, 7);
+    store_img(Pw + PT * fs, b, c, i, j, k, eint, 7);
     store_img(Pw + PMX * fs, b, c, i, j, k, mx, 1);
     store_img(Pw + PMY * fs, b, c, i, j, k, my, 2);
     store_img(Pw + PMZ * fs, b, c, i, j, k, mz, 4);
@@ -339,7 +339,7 @@ __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __rest
     // offsets from the box's reference values, formed in FP64 before rounding to FP32
     const double pd = fma(kGm1 * rho, eint, -sc.p);        // p - p_ref
     const float dp = (float)pd;
-    const float dT = (float)((eint - sc.e) * (1.0 / kCv));  // T - T_ref
+    const float dT = (float)(eint - sc.e);                  // e - e_ref (= c_v (T - T_ref))
     const float dH = (float)(E - sc.E) + dp;                // (E + p) - H_ref
     *health |= health_bits(rho, eint);
     const float pv[NPF] = {u, v, w, dT, mx, my, mz, fmaf(mx, u, dp), fmaf(my, v, dp), fmaf(mz, w, dp),
