@@ -183,7 +183,7 @@ __device__ __forceinline__ bool planes_ready(const volatile int* done, int n0, i
 }
 
 template <bool GHOSTS>
-__global__ void __launch_bounds__(kWarps * 32) k_upload_deriv(BoxView b, double* __restrict__ h,
+__global__ void __launch_bounds__(kWarps * 32, 4) k_upload_deriv(BoxView b, double* __restrict__ h,
                                                                const Tile* __restrict__ tiles,
                                                                const int* __restrict__ queue, int nq, int* counter,
                                                                int* done) {

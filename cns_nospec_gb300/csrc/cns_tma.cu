@@ -846,19 +846,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_deriv_tma(const BoxView* __
             const float ux = d[0][0][i], uy = d[0][1][i], uz = d[0][2][i];
             const float vx = d[1][0][i], vy = d[1][1][i], vz = d[1][2][i];
             const float wx = d[2][0][i], wy = d[2][1][i], wz = d[2][2][i];
-            const float divu = (float)(2.0 / 3.0) * (ux + vy + wz);
-            const float tauxx = fmaf(2.0f, ux, -divu), tauyy = fmaf(2.0f, vy, -divu), tauzz = fmaf(2.0f, wz, -divu);
-            const float tauxy = uy + vx, tauxz = uz + wx, tauyz = vz + wy;
-            float phi = tauxx * ux;
-            phi = fmaf(tauyy, vy, phi);
-            phi = fmaf(tauzz, wz, phi);
-            phi = fmaf(tauxy, tauxy, phi);
-            phi = fmaf(tauxz, tauxz, phi);
-            phi = fmaf(tauyz, tauyz, phi);
+            float sx, sy, sz, phi;
+            dissipation(ux, uy, uz, vx, vy, vz, wx, wy, wz, &sx, &sy, &sz, &phi);
             const long long c = cell_off(b, ic, j, k);
-            store_img(S + SX * fs, b, c, ic, j, k, vy + wz, 1);
-            store_img(S + SY * fs, b, c, ic, j, k, ux + wz, 2);
-            store_img(S + SZ * fs, b, c, ic, j, k, ux + vy, 4);
+            store_img(S + SX * fs, b, c, ic, j, k, sx, 1);
+            store_img(S + SY * fs, b, c, ic, j, k, sy, 2);
+            store_img(S + SZ * fs, b, c, ic, j, k, sz, 4);
             S[SPHI * fs + c] = cf.eta * phi;
         }
     }
