@@ -260,9 +260,11 @@ __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restr
     const double rho = un[0], mx = un[1], my = un[2], mz = un[3], E = un[4];
     const double rinv = rcp_nr(rho);
     const double u = mx * rinv, v = my * rinv, w = mz * rinv;
-    const double ke = fma(u, u, fma(v, v, w * w));
-    const double eint = fma(-0.5, ke, E * rinv);
-    const double p = (kGm1 * eint) * rho;
+    // rho e = E - (rho u u + rho v v + rho w w) / 2 (cpu/ctoprim.cpp's E/rho - |u|^2/2, times rho);
+    // p = (gamma - 1) rho e and e = rho e / rho: one operation fewer than forming E/rho and |u|^2
+    const double re = fma(-0.5, fma(mx, u, fma(my, v, mz * w)), E);
+    const double p = kGm1 * re;
+    const double eint = re * rinv;
     const double H = E + p;
     *health |= health_bits(rho, eint);
     // Field by field, not store_pset: its 16 live FP64 values would cost the upload kernels
