@@ -476,8 +476,10 @@ def run_ours(args, dist):
                      "flops_basis": "the reference's FP64 operation count (2,450 per cell-update, less k_deriv's "
                                     "3 x 132, over 3 launches); the fused kernel retires fewer FP64 instructions "
                                     "than that count, so frac can exceed 1",
-                     "fp64_pipe_busy_ncu": 0.904,
-                     "fp64_pipe_source": "ncu sm__pipe_fp64_cycles_active, profiles/k_assemble_fp64_128cube.md",
+                     "fp64_pipe_busy_ncu": 0.744, "int_pipe_busy_ncu": 0.361,
+                     "pipe_source": "ncu sm__pipe_fp64_cycles_active and sm__inst_executed_pipe_alu of stage 1 "
+                                    "(part of the stencil sums run exactly on the integer pipes), "
+                                    "profiles/k_assemble_fp64_128cube.md",
                      "traffic": traffic, "traffic_source": tsrc},
         "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak, "frac": hbm_gbs / hbm_peak,
                 "bytes_per_cell_update": BYTES_PER_CELL_UPDATE, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},

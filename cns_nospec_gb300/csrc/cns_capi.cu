@@ -214,6 +214,10 @@ static void fill_coefs(BoxView& v, const cns_box_desc* d) {
             c.mx[a][m] = (d->eta * (1.0 / 3.0)) * A[m] * dxi[a];
             c.tl[a][m] = alam_cv * B[m] * (dxi[a] * dxi[a]);
         }
+        c.da[a][4] = dxi[a] / kD1Den;
+        c.ha[a][4] = -dxi[a] / kD1Den;
+        c.mx[a][4] = (d->eta * (1.0 / 3.0)) * dxi[a] / kD1Den;
+        c.tl[a][4] = alam_cv * (dxi[a] * dxi[a]) / kD2Den;
         tsum += dxi[a] * dxi[a];
         c.cour[a] = dxi[a];
     }
@@ -223,6 +227,7 @@ static void fill_coefs(BoxView& v, const cns_box_desc* d) {
         for (int a = 0; a < 3; a++) {
             const double w = d->eta * (comp == a ? 4.0 / 3.0 : 1.0) * (dxi[a] * dxi[a]);
             for (int m = 0; m < 4; m++) c.vl[comp][a][m] = w * B[m];
+            c.vl[comp][a][4] = w / kD2Den;
             sum += w;
         }
         c.vc[comp] = kCenter * sum;

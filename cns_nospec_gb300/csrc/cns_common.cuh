@@ -23,6 +23,9 @@ constexpr double kCv = 8.3333333333e6;
 constexpr double kAlp = 0.8, kBet = -0.2, kGam = 4.0 / 105.0, kDel = -1.0 / 280.0;
 constexpr double kCenter = -205.0 / 72.0, kOff1 = 8.0 / 5.0, kOff2 = -0.2, kOff3 = 8.0 / 315.0,
                  kOff4 = -1.0 / 560.0;
+// The same operators as integer weights over a common denominator (ALP..DEL = 672, -168, 32,
+// -3 over 840; OFF1..OFF4 = 8064, -1008, 128, -9 over 5040), for the exact stencil sums.
+constexpr double kD1Den = 840.0, kD2Den = 5040.0;
 
 // ---- field indices ----------------------------------------------------------------------
 // Conserved state (FP64 always): rho, rho u, rho v, rho w, rho E  (cpu/header.h:20-26).
@@ -50,12 +53,14 @@ enum { SX = 0,   // v_y + w_z  (differenced along x for the mixed terms of the x
 // stencil tap is one fused multiply-add.  Kept in FP64 (plain form) and FP32 (mixed form).
 template <class R>
 struct CoefT {
-    R da[3][4];     // first derivative along d: a_m / dx_d
-    R ha[3][4];     // convective flux divergence: -a_m / dx_d
-    R mx[3][4];     // mixed viscous term: (eta/3) a_m / dx_d
-    R vl[3][3][4];  // viscous Laplacian of velocity c along d: eta (4/3 if c==d) b_m / dx_d^2
+    // Each stencil row holds its four coefficients (weight x factor) and, at [4], the factor
+    // over the weights' denominator (840 or 5040) for the exact sums of the plain form.
+    R da[3][5];     // first derivative along d: a_m / dx_d
+    R ha[3][5];     // convective flux divergence: -a_m / dx_d
+    R mx[3][5];     // mixed viscous term: (eta/3) a_m / dx_d
+    R vl[3][3][5];  // viscous Laplacian of velocity c along d: eta (4/3 if c==d) b_m / dx_d^2
     R vc[3];        // its centre weight: eta c0 sum_d (4/3 if c==d) / dx_d^2
-    R tl[3][4];     // heat conduction along d: (alam / c_v) b_m / dx_d^2, applied to e = c_v T
+    R tl[3][5];     // heat conduction along d: (alam / c_v) b_m / dx_d^2, applied to e = c_v T
     R tc;           // (alam / c_v) c0 sum_d 1/dx_d^2
     R cour[3];      // 1/dx_d (Courant number)
     R eta;          // viscosity

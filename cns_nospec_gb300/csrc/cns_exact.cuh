@@ -1,0 +1,191 @@
+// Exact 8-tap stencil sums for the plain FP64 form, on the integer pipes.
+//
+// On GB300 an FP64 instruction holds the FP64 pipe about 64 times longer than an FP32 or
+// integer one, and the plain kernels are bound by that pipe.  The stencils of the 8th-order
+// operators have small integer weights over a common denominator:
+//   first derivative  (ALP, BET, GAM, DEL)     = ( 672, -168,  32, -3) / 840
+//   second derivative (OFF1, OFF2, OFF3, OFF4) = (8064, -1008, 128, -9) / 5040
+// (cpu/header.h:88-91, cpu/diffterm.cpp:48-52), so sum_m w_m (f[+m] -+ f[-m]) can be formed
+// exactly in integers: each tap's 53-bit significand is placed 9 bits below the ulp of the
+// largest tap (a tap more than 9 binades smaller keeps its bits down to 2^-62 of the largest
+// one), split into two 31-bit halves, multiplied by its signed weight and summed in two 64-bit
+// accumulators (one wide multiply-add per half), then rounded once to FP64, to nearest even.
+// The caller scales the sum by its per-axis factor (coefficient / 840 or / 5040) in one FP64
+// FMA: one FP64 instruction per stencil instead of eight, and a sum that is correctly rounded
+// where the FP64 chain rounds eight times.  Taps that are not finite, or sums outside the normal
+// range (taps above ~2^1000 or below ~2^-960), report failure; the caller then takes the FP64
+// chain, so every input gives what FP64 arithmetic gives.
+#pragma once
+#include <cstring>
+
+#include "cns_common.cuh"
+
+namespace cns {
+
+__host__ __device__ __forceinline__ int xhi(double v) {
+#ifdef __CUDA_ARCH__
+    return __double2hiint(v);
+#else
+    unsigned long long u;
+    memcpy(&u, &v, 8);
+    return (int)(u >> 32);
+#endif
+}
+__host__ __device__ __forceinline__ unsigned xlo(double v) {
+#ifdef __CUDA_ARCH__
+    return (unsigned)__double2loint(v);
+#else
+    unsigned long long u;
+    memcpy(&u, &v, 8);
+    return (unsigned)u;
+#endif
+}
+__host__ __device__ __forceinline__ double xbits(unsigned long long u) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    double v;
+    memcpy(&v, &u, 8);
+    return v;
+#endif
+}
+__host__ __device__ __forceinline__ int xclz64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+constexpr int kXGuard = 9;  // guard bits below the largest tap's ulp
+
+// Which stencils of the plain form take the exact sums (the others the FP64 chain), as masks
+// over the axes (bit d: along d): the first derivatives of the derivative pass, those of the
+// flux divergence, those of the mixed viscous terms, the Laplacian second differences.  The
+// integer and FP64 pipes work side by side, so the best split keeps both busy.
+constexpr int kExactDeriv = 0b110, kExactFlux = 0b100, kExactMixed = 0, kExactLap = 0b110;
+constexpr bool xon(int mask, int axis) { return (mask >> axis) & 1; }
+
+// The exponent field (bits 20-30 of the high word) of the largest of a set of taps, at least 1
+// (zeros and subnormals share the scale of exponent 1).
+__host__ __device__ __forceinline__ int xfield(double v) { return xhi(v) & 0x7FF00000; }
+__host__ __device__ __forceinline__ int xmax(int a, int b) { return a > b ? a : b; }
+
+// One tap of weight w into the accumulators, at the scale of exponent emax.
+__host__ __device__ __forceinline__ void xtap(long long& L, long long& H, double v, int emax, int w) {
+    const int hi = xhi(v);
+    const int e = (hi >> 20) & 0x7FF;
+    const unsigned mh = ((unsigned)hi & 0xFFFFFu) | (e ? 0x100000u : 0u);
+    int sh = emax - (e > 1 ? e : 1);
+    sh = sh < 63 ? sh : 63;
+    const unsigned long long t = ((((unsigned long long)mh << 32) | xlo(v)) << kXGuard) >> sh;  // < 2^62
+    const int s = hi >> 31;
+    const int ws = (w ^ s) - s;  // the weight of the tap's value, sign included
+    L += (long long)ws * (int)((unsigned)t & 0x7FFFFFFFu);
+    H += (long long)ws * (int)(t >> 31);
+}
+
+// (H * 2^31 + L) * 2^e2 rounded to nearest even; false when outside the normal range.
+__host__ __device__ __forceinline__ bool xround(long long H, long long L, int e2, double* out) {
+    H += L >> 31;
+    const unsigned l = (unsigned)L & 0x7FFFFFFFu;  // S = H 2^31 + l, 0 <= l < 2^31
+    const bool neg = H < 0;
+    // |S| = mh 2^31 + ml with ml < 2^31
+    const unsigned long long mh = !neg ? (unsigned long long)H : (l ? (unsigned long long)~H : (unsigned long long)-H);
+    const unsigned ml = !neg ? l : (l ? 0x80000000u - l : 0u);
+    if (mh == 0 && ml == 0) {
+        *out = 0.0;
+        return true;
+    }
+    unsigned long long top;  // |S| with its leading bit at 63
+    bool sticky = false;
+    int p;  // position of the leading bit of |S|
+    if (mh) {
+        const int z = xclz64(mh);  // >= 15: |H| < 2^49
+        p = 94 - z;
+        if (z <= 31) {
+            const int r = 31 - z;
+            top = (mh << z) | ((unsigned long long)ml >> r);
+            sticky = (ml & ((1u << r) - 1u)) != 0;
+        } else {
+            top = (mh << z) | ((unsigned long long)ml << (z - 31));
+        }
+    } else {
+        const int z = xclz64((unsigned long long)ml);  // >= 33
+        p = 63 - z;
+        top = (unsigned long long)ml << z;
+    }
+    unsigned long long q = top >> 11;
+    const unsigned rem = (unsigned)top & 0x7FFu;
+    q += (rem > 0x400u || (rem == 0x400u && (sticky || (q & 1ull)))) ? 1ull : 0ull;
+    const int be = p + e2 + 1023;
+    if (be < 1 || be > 2045) return false;
+    *out = xbits(((unsigned long long)(be - 1) << 52) + q | (neg ? 0x8000000000000000ull : 0ull));
+    return true;
+}
+
+// sum_{m=1..4} w_m (ld(m) + SGN ld(-m)), exactly, rounded once; false (and *out untouched)
+// for taps that are not finite or a sum outside the normal range.  ld(m) returns the tap at
+// offset m; SGN = -1 for first derivatives, +1 for the off-centre part of second derivatives.
+template <int W1, int W2, int W3, int W4, int SGN, class Ld>
+__host__ __device__ __forceinline__ bool xsum8(const Ld& ld, double* out) {
+    const double a1 = ld(1), a2 = ld(2), a3 = ld(3), a4 = ld(4);
+    const double b1 = ld(-1), b2 = ld(-2), b3 = ld(-3), b4 = ld(-4);
+    int f = 0x00100000;
+    f = xmax(f, xfield(a1));
+    f = xmax(f, xfield(b1));
+    f = xmax(f, xfield(a2));
+    f = xmax(f, xfield(b2));
+    f = xmax(f, xfield(a3));
+    f = xmax(f, xfield(b3));
+    f = xmax(f, xfield(a4));
+    f = xmax(f, xfield(b4));
+    const int emax = f >> 20;
+    if (emax == 0x7FF) return false;
+    long long L = 0, H = 0;
+    xtap(L, H, a1, emax, W1);
+    xtap(L, H, b1, emax, SGN * W1);
+    xtap(L, H, a2, emax, W2);
+    xtap(L, H, b2, emax, SGN * W2);
+    xtap(L, H, a3, emax, W3);
+    xtap(L, H, b3, emax, SGN * W3);
+    xtap(L, H, a4, emax, W4);
+    xtap(L, H, b4, emax, SGN * W4);
+    return xround(H, L, emax - 1075 - kXGuard, out);
+}
+
+// The exact stencils with their FP64 fallbacks.  a[0..3] are the chain's coefficients
+// (weights / denominator x factor), a[4] = factor / denominator.
+template <class Ld>
+__host__ __device__ __forceinline__ double xd1acc(double acc, const Ld& ld, const double* a) {
+    double x;
+    if (xsum8<672, -168, 32, -3, -1>(ld, &x)) return fma(a[4], x, acc);
+    acc = fma(a[0], ld(1) - ld(-1), acc);
+    acc = fma(a[1], ld(2) - ld(-2), acc);
+    acc = fma(a[2], ld(3) - ld(-3), acc);
+    return fma(a[3], ld(4) - ld(-4), acc);
+}
+template <class Ld>
+__host__ __device__ __forceinline__ double xd2acc(double acc, const Ld& ld, const double* b) {
+    double x;
+    if (xsum8<8064, -1008, 128, -9, 1>(ld, &x)) return fma(b[4], x, acc);
+    acc = fma(b[0], ld(1) + ld(-1), acc);
+    acc = fma(b[1], ld(2) + ld(-2), acc);
+    acc = fma(b[2], ld(3) + ld(-3), acc);
+    return fma(b[3], ld(4) + ld(-4), acc);
+}
+
+// Tap loaders: a strided array (global memory through a chosen load, or shared memory) and a
+// register column.
+template <int MODE>  // 0: read-only path, 1: L2 (data written during the launch), 2: plain
+struct XTaps {
+    const double* p;
+    long long s;
+    __device__ __forceinline__ double operator()(int m) const {
+        if (MODE == 0) return __ldg(p + m * s);
+        if (MODE == 1) return __ldcg(p + m * s);
+        return p[m * s];
+    }
+};
+
+}  // namespace cns

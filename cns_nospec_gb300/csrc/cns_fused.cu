@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kTileThreads) k_prim(const BoxView* __restrict
 
 // ---- k_deriv: first derivatives of (u,v,w) -> mixed-term sums and viscous dissipation -------
 template <class R>
-__global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
+__global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
                                                       int ntiles, int stage) {
     pdl_enter();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kTileThreads) k_deriv(const BoxView* __restric
 
 // ---- k_assemble: D + F, RK stage combine, fused ctoprim/flux/ghost write-back -------------
 template <class R, int STAGE>
-__global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __restrict__ boxes,
+__global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __restrict__ boxes,
                                                          const Tile* __restrict__ tiles, int ntiles) {
     pdl_enter();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -81,45 +81,45 @@ __global__ void __launch_bounds__(kTileThreads) k_assemble(const BoxView* __rest
             const R u0 = ld(pu), v0 = ld(pv), w0 = ld(pw), t0 = ld(pt);
             // diffterm momentum components (cpu/diffterm.cpp:155-269)
             R dmx = cf.vc[0] * u0;
-            dmx = d2acc(dmx, pu, si, cf.vl[0][0]);
-            dmx = d2acc(dmx, pu, sj, cf.vl[0][1]);
-            dmx = d2acc(dmx, pu, 1, cf.vl[0][2]);
-            dmx = d1acc(dmx, S + SX * fs + c, si, cf.mx[0]);
+            dmx = d2acc<xon(kExactLap, 0)>(dmx, pu, si, cf.vl[0][0]);
+            dmx = d2acc<xon(kExactLap, 1)>(dmx, pu, sj, cf.vl[0][1]);
+            dmx = d2acc<xon(kExactLap, 2)>(dmx, pu, 1, cf.vl[0][2]);
+            dmx = d1acc<xon(kExactMixed, 0)>(dmx, S + SX * fs + c, si, cf.mx[0]);
             R dmy = cf.vc[1] * v0;
-            dmy = d2acc(dmy, pv, si, cf.vl[1][0]);
-            dmy = d2acc(dmy, pv, sj, cf.vl[1][1]);
-            dmy = d2acc(dmy, pv, 1, cf.vl[1][2]);
-            dmy = d1acc(dmy, S + SY * fs + c, sj, cf.mx[1]);
+            dmy = d2acc<xon(kExactLap, 0)>(dmy, pv, si, cf.vl[1][0]);
+            dmy = d2acc<xon(kExactLap, 1)>(dmy, pv, sj, cf.vl[1][1]);
+            dmy = d2acc<xon(kExactLap, 2)>(dmy, pv, 1, cf.vl[1][2]);
+            dmy = d1acc<xon(kExactMixed, 1)>(dmy, S + SY * fs + c, sj, cf.mx[1]);
             R dmz = cf.vc[2] * w0;
-            dmz = d2acc(dmz, pw, si, cf.vl[2][0]);
-            dmz = d2acc(dmz, pw, sj, cf.vl[2][1]);
-            dmz = d2acc(dmz, pw, 1, cf.vl[2][2]);
-            dmz = d1acc(dmz, S + SZ * fs + c, 1, cf.mx[2]);
+            dmz = d2acc<xon(kExactLap, 0)>(dmz, pw, si, cf.vl[2][0]);
+            dmz = d2acc<xon(kExactLap, 1)>(dmz, pw, sj, cf.vl[2][1]);
+            dmz = d2acc<xon(kExactLap, 2)>(dmz, pw, 1, cf.vl[2][2]);
+            dmz = d1acc<xon(kExactMixed, 2)>(dmz, S + SZ * fs + c, 1, cf.mx[2]);
             // diffterm energy component (cpu/diffterm.cpp:272-311)
             R de = fma(cf.tc, t0, ld(S + SPHI * fs + c));
-            de = d2acc(de, pt, si, cf.tl[0]);
-            de = d2acc(de, pt, sj, cf.tl[1]);
-            de = d2acc(de, pt, 1, cf.tl[2]);
+            de = d2acc<xon(kExactLap, 0)>(de, pt, si, cf.tl[0]);
+            de = d2acc<xon(kExactLap, 1)>(de, pt, sj, cf.tl[1]);
+            de = d2acc<xon(kExactLap, 2)>(de, pt, 1, cf.tl[2]);
             de = fma(dmx, u0, de);
             de = fma(dmy, v0, de);
             de = fma(dmz, w0, de);
             // hypterm (cpu/hypterm.cpp:29-208), added to D
             R f[5];
-            f[0] = d1(Pr + PMX * fs + c, si, cf.ha[0]);
-            f[0] = d1acc(f[0], Pr + PMY * fs + c, sj, cf.ha[1]);
-            f[0] = d1acc(f[0], Pr + PMZ * fs + c, 1, cf.ha[2]);
-            f[1] = d1acc(dmx, Pr + PFUU * fs + c, si, cf.ha[0]);
-            f[1] = d1acc(f[1], Pr + PFUV * fs + c, sj, cf.ha[1]);
-            f[1] = d1acc(f[1], Pr + PFUW * fs + c, 1, cf.ha[2]);
-            f[2] = d1acc(dmy, Pr + PFUV * fs + c, si, cf.ha[0]);
-            f[2] = d1acc(f[2], Pr + PFVV * fs + c, sj, cf.ha[1]);
-            f[2] = d1acc(f[2], Pr + PFVW * fs + c, 1, cf.ha[2]);
-            f[3] = d1acc(dmz, Pr + PFUW * fs + c, si, cf.ha[0]);
-            f[3] = d1acc(f[3], Pr + PFVW * fs + c, sj, cf.ha[1]);
-            f[3] = d1acc(f[3], Pr + PFWW * fs + c, 1, cf.ha[2]);
-            f[4] = d1acc(de, Pr + PHU * fs + c, si, cf.ha[0]);
-            f[4] = d1acc(f[4], Pr + PHV * fs + c, sj, cf.ha[1]);
-            f[4] = d1acc(f[4], Pr + PHW * fs + c, 1, cf.ha[2]);
+            f[0] = d1<xon(kExactFlux, 0)>(Pr + PMX * fs + c, si, cf.ha[0]);
+            f[0] = d1acc<xon(kExactFlux, 1)>(f[0], Pr + PMY * fs + c, sj, cf.ha[1]);
+            f[0] = d1acc<xon(kExactFlux, 2)>(f[0], Pr + PMZ * fs + c, 1, cf.ha[2]);
+            f[1] = d1acc<xon(kExactFlux, 0)>(dmx, Pr + PFUU * fs + c, si, cf.ha[0]);
+            f[1] = d1acc<xon(kExactFlux, 1)>(f[1], Pr + PFUV * fs + c, sj, cf.ha[1]);
+            f[1] = d1acc<xon(kExactFlux, 2)>(f[1], Pr + PFUW * fs + c, 1, cf.ha[2]);
+            f[2] = d1acc<xon(kExactFlux, 0)>(dmy, Pr + PFUV * fs + c, si, cf.ha[0]);
+            f[2] = d1acc<xon(kExactFlux, 1)>(f[2], Pr + PFVV * fs + c, sj, cf.ha[1]);
+            f[2] = d1acc<xon(kExactFlux, 2)>(f[2], Pr + PFVW * fs + c, 1, cf.ha[2]);
+            f[3] = d1acc<xon(kExactFlux, 0)>(dmz, Pr + PFUW * fs + c, si, cf.ha[0]);
+            f[3] = d1acc<xon(kExactFlux, 1)>(f[3], Pr + PFVW * fs + c, sj, cf.ha[1]);
+            f[3] = d1acc<xon(kExactFlux, 2)>(f[3], Pr + PFWW * fs + c, 1, cf.ha[2]);
+            f[4] = d1acc<xon(kExactFlux, 0)>(de, Pr + PHU * fs + c, si, cf.ha[0]);
+            f[4] = d1acc<xon(kExactFlux, 1)>(f[4], Pr + PHV * fs + c, sj, cf.ha[1]);
+            f[4] = d1acc<xon(kExactFlux, 2)>(f[4], Pr + PHW * fs + c, 1, cf.ha[2]);
             if (sizeof(R) == 4) {
                 // mixed form: the P set holds ((E + p) - H_ref) u_d, so add -H_ref div(u);
                 // div(u) = (S_x + S_y + S_z) / 2 with the same first-difference operator

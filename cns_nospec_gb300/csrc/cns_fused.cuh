@@ -17,7 +17,9 @@
 // GB300's FP64 rate is 1/67 of its FP32 rate, so the plain form is bound by the FP64 pipe,
 // not by HBM: the kernels are arranged so that every FP64 quantity is computed exactly once
 // per cell (no halo recomputation of primitives or derivatives) and every stencil tap is one
-// FMA with a coefficient pre-folded with 1/dx, eta or alam.
+// FMA with a coefficient pre-folded with 1/dx, eta or alam.  Part of the stencils (chosen per
+// family and axis, cns_exact.cuh) are instead summed exactly on the integer pipes and cost one
+// FP64 instruction each, so that the integer and FP64 pipes share the work.
 //
 // Algebraic regrouping against the reference (same discrete operators; rounding differs at
 // the level of a few ulp):
@@ -29,6 +31,7 @@
 //   * the three second differences of each Laplacian share one centre tap.
 #pragma once
 #include "cns_common.cuh"
+#include "cns_exact.cuh"
 
 namespace cns {
 
@@ -39,9 +42,10 @@ __device__ __forceinline__ const CoefT<double>& coefs<double>(const BoxView& b) 
 template <>
 __device__ __forceinline__ const CoefT<float>& coefs<float>(const BoxView& b) { return b.c32; }
 
-// acc + sum_m a_m (p[m s] - p[-m s])
-template <class R>
+// acc + sum_m a_m (p[m s] - p[-m s]); in the plain form (R = double) the exact sum (cns_exact.cuh)
+template <bool X, class R>
 __device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, const R* a) {
+    if constexpr (sizeof(R) == 8 && X) return xd1acc(acc, XTaps<0>{p, s}, a);
     acc = fma(a[0], __ldg(p + s) - __ldg(p - s), acc);
     acc = fma(a[1], __ldg(p + 2 * s) - __ldg(p - 2 * s), acc);
     acc = fma(a[2], __ldg(p + 3 * s) - __ldg(p - 3 * s), acc);
@@ -56,8 +60,9 @@ __device__ __forceinline__ R ld_tap(const R* p) {
     if (NC) return __ldg(p);
     return __ldcg(p);
 }
-template <class R, bool NC = true>
+template <bool X, class R, bool NC = true>
 __device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a) {
+    if constexpr (sizeof(R) == 8 && X) return xd1acc(0.0, XTaps<NC ? 0 : 1>{p, s}, a);
     R acc = a[0] * (ld_tap<NC>(p + s) - ld_tap<NC>(p - s));
     acc = fma(a[1], ld_tap<NC>(p + 2 * s) - ld_tap<NC>(p - 2 * s), acc);
     acc = fma(a[2], ld_tap<NC>(p + 3 * s) - ld_tap<NC>(p - 3 * s), acc);
@@ -65,8 +70,9 @@ __device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a
     return acc;
 }
 // acc + sum_m b_m (p[m s] + p[-m s])
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R d2acc(R acc, const R* __restrict__ p, long long s, const R* b) {
+    if constexpr (sizeof(R) == 8 && X) return xd2acc(acc, XTaps<0>{p, s}, b);
     acc = fma(b[0], __ldg(p + s) + __ldg(p - s), acc);
     acc = fma(b[1], __ldg(p + 2 * s) + __ldg(p - 2 * s), acc);
     acc = fma(b[2], __ldg(p + 3 * s) + __ldg(p - 3 * s), acc);
@@ -166,9 +172,10 @@ __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k
     const R* pu = P + PU * fs + c;
     const R* pv = P + PV * fs + c;
     const R* pw = P + PW * fs + c;
-    const R ux = d1<R, NC>(pu, si, cf.da[0]), uy = d1<R, NC>(pu, sj, cf.da[1]), uz = d1<R, NC>(pu, 1, cf.da[2]);
-    const R vx = d1<R, NC>(pv, si, cf.da[0]), vy = d1<R, NC>(pv, sj, cf.da[1]), vz = d1<R, NC>(pv, 1, cf.da[2]);
-    const R wx = d1<R, NC>(pw, si, cf.da[0]), wy = d1<R, NC>(pw, sj, cf.da[1]), wz = d1<R, NC>(pw, 1, cf.da[2]);
+    constexpr bool X0 = xon(kExactDeriv, 0), X1 = xon(kExactDeriv, 1), X2 = xon(kExactDeriv, 2);
+    const R ux = d1<X0, R, NC>(pu, si, cf.da[0]), uy = d1<X1, R, NC>(pu, sj, cf.da[1]), uz = d1<X2, R, NC>(pu, 1, cf.da[2]);
+    const R vx = d1<X0, R, NC>(pv, si, cf.da[0]), vy = d1<X1, R, NC>(pv, sj, cf.da[1]), vz = d1<X2, R, NC>(pv, 1, cf.da[2]);
+    const R wx = d1<X0, R, NC>(pw, si, cf.da[0]), wy = d1<X1, R, NC>(pw, sj, cf.da[1]), wz = d1<X2, R, NC>(pw, 1, cf.da[2]);
     R sx, sy, sz, phi;
     dissipation(ux, uy, uz, vx, vy, vz, wx, wy, wz, &sx, &sy, &sz, &phi);
     store_img(S + SX * fs, b, c, i, j, k, sx, 1);

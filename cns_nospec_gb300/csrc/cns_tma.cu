@@ -145,24 +145,27 @@ __device__ __forceinline__ void prefetch_state_l2(const BoxView& b, const Tile& 
     }
 }
 
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R sd1acc(R acc, const R* p, int s, const R* a) {
+    if constexpr (sizeof(R) == 8 && X) return xd1acc(acc, XTaps<2>{p, s}, a);
     acc = fma(a[0], p[s] - p[-s], acc);
     acc = fma(a[1], p[2 * s] - p[-2 * s], acc);
     acc = fma(a[2], p[3 * s] - p[-3 * s], acc);
     acc = fma(a[3], p[4 * s] - p[-4 * s], acc);
     return acc;
 }
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R sd1(const R* p, int s, const R* a) {
+    if constexpr (sizeof(R) == 8 && X) return xd1acc(0.0, XTaps<2>{p, s}, a);
     R acc = a[0] * (p[s] - p[-s]);
     acc = fma(a[1], p[2 * s] - p[-2 * s], acc);
     acc = fma(a[2], p[3 * s] - p[-3 * s], acc);
     acc = fma(a[3], p[4 * s] - p[-4 * s], acc);
     return acc;
 }
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R sd2acc(R acc, const R* p, int s, const R* b) {
+    if constexpr (sizeof(R) == 8 && X) return xd2acc(acc, XTaps<2>{p, s}, b);
     acc = fma(b[0], p[s] + p[-s], acc);
     acc = fma(b[1], p[2 * s] + p[-2 * s], acc);
     acc = fma(b[2], p[3 * s] + p[-3 * s], acc);
@@ -170,24 +173,27 @@ __device__ __forceinline__ R sd2acc(R acc, const R* p, int s, const R* b) {
     return acc;
 }
 // the same on a register column (i direction), centre index c
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R cd1acc(R acc, const R* col, int c, const R* a) {
+    if constexpr (sizeof(R) == 8 && X) return xd1acc(acc, [&](int m) { return col[c + m]; }, a);
     acc = fma(a[0], col[c + 1] - col[c - 1], acc);
     acc = fma(a[1], col[c + 2] - col[c - 2], acc);
     acc = fma(a[2], col[c + 3] - col[c - 3], acc);
     acc = fma(a[3], col[c + 4] - col[c - 4], acc);
     return acc;
 }
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R cd1(const R* col, int c, const R* a) {
+    if constexpr (sizeof(R) == 8 && X) return xd1acc(0.0, [&](int m) { return col[c + m]; }, a);
     R acc = a[0] * (col[c + 1] - col[c - 1]);
     acc = fma(a[1], col[c + 2] - col[c - 2], acc);
     acc = fma(a[2], col[c + 3] - col[c - 3], acc);
     acc = fma(a[3], col[c + 4] - col[c - 4], acc);
     return acc;
 }
-template <class R>
+template <bool X, class R>
 __device__ __forceinline__ R cd2acc(R acc, const R* col, int c, const R* b) {
+    if constexpr (sizeof(R) == 8 && X) return xd2acc(acc, [&](int m) { return col[c + m]; }, b);
     acc = fma(b[0], col[c + 1] + col[c - 1], acc);
     acc = fma(b[1], col[c + 2] + col[c - 2], acc);
     acc = fma(b[2], col[c + 3] + col[c - 3], acc);
@@ -208,10 +214,10 @@ __device__ __forceinline__ void lap_full(const R* s, int tj, int tk, R cw, const
         const R c0 = col[i + 4];
         ctr[i] = c0;
         R a = init_from_acc ? fma(cw, c0, acc[i]) : cw * c0;
-        a = cd2acc(a, col, i + 4, wi);
+        a = cd2acc<xon(kExactLap, 0)>(a, col, i + 4, wi);
         const R* p = s + B::at(i + 4, tj + 4, tk + 4);
-        a = sd2acc(a, p, B::K, wj);
-        a = sd2acc(a, p, 1, wk);
+        a = sd2acc<xon(kExactLap, 1)>(a, p, B::K, wj);
+        a = sd2acc<xon(kExactLap, 2)>(a, p, 1, wk);
         acc[i] = a;
     }
 }
@@ -245,7 +251,7 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
             for (int i = 0; i < XI; i++) {
-                dmx[i] = cd1acc(dmx[i], col, i + 4, cf.mx[0]);
+                dmx[i] = cd1acc<xon(kExactMixed, 0)>(dmx[i], col, i + 4, cf.mx[0]);
                 de[i] = fma(dmx[i], c0[i], de[i]);
             }
             break;
@@ -257,7 +263,7 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
             using B = Bx<BX_J>;
 #pragma unroll
             for (int i = 0; i < XI; i++) {
-                dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
+                dmy[i] = sd1acc<xon(kExactMixed, 1)>(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
                 de[i] = fma(dmy[i], c0[i], de[i]);
             }
             break;
@@ -269,7 +275,7 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
             using B = Bx<BX_K>;
 #pragma unroll
             for (int i = 0; i < XI; i++) {
-                dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.mx[2]);
+                dmz[i] = sd1acc<xon(kExactMixed, 2)>(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.mx[2]);
                 de[i] = fma(dmz[i], c0[i], de[i]);
             }
             break;
@@ -280,19 +286,19 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
-            for (int i = 0; i < XI; i++) f0[i] = cd1(col, i + 4, cf.ha[0]);
+            for (int i = 0; i < XI; i++) f0[i] = cd1<xon(kExactFlux, 0)>(col, i + 4, cf.ha[0]);
             break;
         }
         case 9: {  // PMY
             using B = Bx<BX_J>;
 #pragma unroll
-            for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+            for (int i = 0; i < XI; i++) f0[i] = sd1acc<xon(kExactFlux, 1)>(f0[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
             break;
         }
         case 10: {  // PMZ
             using B = Bx<BX_K>;
 #pragma unroll
-            for (int i = 0; i < XI; i++) f0[i] = sd1acc(f0[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+            for (int i = 0; i < XI; i++) f0[i] = sd1acc<xon(kExactFlux, 2)>(f0[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
             break;
         }
         case 11: {  // PFUU along x -> f1 (in dmx)
@@ -301,7 +307,7 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
-            for (int i = 0; i < XI; i++) dmx[i] = cd1acc(dmx[i], col, i + 4, cf.ha[0]);
+            for (int i = 0; i < XI; i++) dmx[i] = cd1acc<xon(kExactFlux, 0)>(dmx[i], col, i + 4, cf.ha[0]);
             break;
         }
         case 12: {  // PFUV: along y -> f1, along x -> f2 (in dmy)
@@ -311,8 +317,8 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj + 4, tk)];
 #pragma unroll
             for (int i = 0; i < XI; i++) {
-                dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj + 4, tk), B::K, cf.ha[1]);
-                dmy[i] = cd1acc(dmy[i], col, i + 4, cf.ha[0]);
+                dmx[i] = sd1acc<xon(kExactFlux, 1)>(dmx[i], s + B::at(i + 4, tj + 4, tk), B::K, cf.ha[1]);
+                dmy[i] = cd1acc<xon(kExactFlux, 0)>(dmy[i], col, i + 4, cf.ha[0]);
             }
             break;
         }
@@ -323,15 +329,15 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk + 4)];
 #pragma unroll
             for (int i = 0; i < XI; i++) {
-                dmx[i] = sd1acc(dmx[i], s + B::at(i + 4, tj, tk + 4), 1, cf.ha[2]);
-                dmz[i] = cd1acc(dmz[i], col, i + 4, cf.ha[0]);
+                dmx[i] = sd1acc<xon(kExactFlux, 2)>(dmx[i], s + B::at(i + 4, tj, tk + 4), 1, cf.ha[2]);
+                dmz[i] = cd1acc<xon(kExactFlux, 0)>(dmz[i], col, i + 4, cf.ha[0]);
             }
             break;
         }
         case 14: {  // PFVV along y -> f2
             using B = Bx<BX_J>;
 #pragma unroll
-            for (int i = 0; i < XI; i++) dmy[i] = sd1acc(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+            for (int i = 0; i < XI; i++) dmy[i] = sd1acc<xon(kExactFlux, 1)>(dmy[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
             break;
         }
         case 15: {  // PFVW: along z -> f2, along y -> f3
@@ -339,15 +345,15 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
 #pragma unroll
             for (int i = 0; i < XI; i++) {
                 const R* p = s + B::at(i, tj + 4, tk + 4);
-                dmy[i] = sd1acc(dmy[i], p, 1, cf.ha[2]);
-                dmz[i] = sd1acc(dmz[i], p, B::K, cf.ha[1]);
+                dmy[i] = sd1acc<xon(kExactFlux, 2)>(dmy[i], p, 1, cf.ha[2]);
+                dmz[i] = sd1acc<xon(kExactFlux, 1)>(dmz[i], p, B::K, cf.ha[1]);
             }
             break;
         }
         case 16: {  // PFWW along z -> f3
             using B = Bx<BX_K>;
 #pragma unroll
-            for (int i = 0; i < XI; i++) dmz[i] = sd1acc(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+            for (int i = 0; i < XI; i++) dmz[i] = sd1acc<xon(kExactFlux, 2)>(dmz[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
             break;
         }
         case 17: {  // PHU along x -> f4 (in de)
@@ -356,13 +362,13 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
 #pragma unroll
             for (int ii = 0; ii < 16; ii++) col[ii] = s[B::at(ii, tj, tk)];
 #pragma unroll
-            for (int i = 0; i < XI; i++) de[i] = cd1acc(de[i], col, i + 4, cf.ha[0]);
+            for (int i = 0; i < XI; i++) de[i] = cd1acc<xon(kExactFlux, 0)>(de[i], col, i + 4, cf.ha[0]);
             break;
         }
         case 18: {  // PHV
             using B = Bx<BX_J>;
 #pragma unroll
-            for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
+            for (int i = 0; i < XI; i++) de[i] = sd1acc<xon(kExactFlux, 1)>(de[i], s + B::at(i, tj + 4, tk), B::K, cf.ha[1]);
             break;
         }
         default: {  // 19, PHW; for mixed boxes then -H_ref div(u) (their P set holds
@@ -377,12 +383,12 @@ __device__ __forceinline__ void consume_field(int e, const R* s, const Tile& T, 
                 for (int i = 0; i < XI; i++) {
                     const long long c = cell_off(b, min(T.i0 + i, b.n[0] - 1), j, k);
                     const float hsum = __ldg(S + SX * b.fs + c) + __ldg(S + SY * b.fs + c) + __ldg(S + SZ * b.fs + c);
-                    const float a = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                    const float a = sd1acc<xon(kExactFlux, 2)>(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
                     de[i] = fmaf(href, 0.5f * hsum, a);
                 }
             } else {
 #pragma unroll
-                for (int i = 0; i < XI; i++) de[i] = sd1acc(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
+                for (int i = 0; i < XI; i++) de[i] = sd1acc<xon(kExactFlux, 2)>(de[i], s + B::at(i, tj, tk + 4), 1, cf.ha[2]);
             }
             break;
         }
@@ -829,9 +835,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_deriv_tma(const BoxView* __
 #pragma unroll
             for (int i = 0; i < XI; i++) {
                 const float* p = s + B::at(i + 4, tj + 4, tk + 4);
-                d[e][0][i] = cd1(col, i + 4, cf.da[0]);
-                d[e][1][i] = sd1(p, B::K, cf.da[1]);
-                d[e][2][i] = sd1(p, 1, cf.da[2]);
+                d[e][0][i] = cd1<xon(kExactDeriv, 0)>(col, i + 4, cf.da[0]);
+                d[e][1][i] = sd1<xon(kExactDeriv, 1)>(p, B::K, cf.da[1]);
+                d[e][2][i] = sd1<xon(kExactDeriv, 2)>(p, 1, cf.da[2]);
             }
             __syncthreads();  // buffer g & 1 is free for load g + 2
         }
