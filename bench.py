@@ -462,6 +462,8 @@ def run_ours(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": box_workload(n),
                    "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
+                   "arithmetic": "FP64; 19 of the 39 8-tap stencil sums per cell and stage formed exactly in "
+                                 "64-bit integers on the significands and rounded once to FP64",
                    "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
                    "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)},
                    "mixed_assembly_kernel": {C.CNS_ASSEMBLE_TMA: "tma", C.CNS_ASSEMBLE_TMA_WS: "tma_ws"}.get(kern32, "direct")},
