@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_host_ghosts(BoxView b, double* 
 // fence before counting it; a tile fences after seeing its counts and reads the P set from L2
 // (deriv_cell<double, false>: it is written during this launch).
 constexpr int kPlaneStart = CNS_NG;  // plane order: q = (i + 4) mod n
-constexpr int kDerivLag = 8;         // planes (measured at 128^3: 4.68 ms per call, 4.85 unfused)
+constexpr int kDerivLag = 8;         // planes (at 128^3 lags of 4 to 16 planes time the same)
 
 __device__ __forceinline__ bool planes_ready(const volatile int* done, int n0, int lo, int hi, int target) {
     for (int p = lo; p <= hi; p++)
