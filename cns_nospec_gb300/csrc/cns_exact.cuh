@@ -12,9 +12,9 @@
 // accumulators (one wide multiply-add per half), then rounded once to FP64, to nearest even.
 // The caller scales the sum by its per-axis factor (coefficient / 840 or / 5040) in one FP64
 // FMA: one FP64 instruction per stencil instead of eight, and a sum that is correctly rounded
-// where the FP64 chain rounds eight times.  Taps that are not finite, or sums outside the normal
-// range (taps above ~2^1000 or below ~2^-960), report failure; the caller then takes the FP64
-// chain, so every input gives what FP64 arithmetic gives.
+// where the FP64 chain rounds eight times.  Taps that are not finite, and nonzero sums outside
+// FP64's normal range (|sum| below 2^-1022 or at least 2^1023), report failure; the caller then
+// takes the FP64 chain, so every input gives what FP64 arithmetic gives.
 #pragma once
 #include <cstring>
 
