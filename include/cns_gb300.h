@@ -46,7 +46,7 @@ typedef enum cns_health {
 } cns_health;
 
 typedef enum cns_precision {
-    CNS_FP64 = 0, /* plain form: FP64 throughout */
+    CNS_FP64 = 0, /* plain form: FP64 state and arithmetic; part of the stencil sums exact in integers, rounded once to FP64 */
     CNS_MIXED = 1 /* FP32 primitives/stencils/fluxes; FP64 e = E/rho - |u|^2/2 and RK3 state */
 } cns_precision;
 
