@@ -54,6 +54,7 @@ SIGNATURES = {
     "cns_device_synchronize": (C.c_int, []),
     "cns_measure_fp64_peak": (C.c_int, [_D]),
     "cns_selftest_bounded_wait": (C.c_int, [_I]),
+    "cns_selftest_exact_sums": (C.c_int, [_D, C.c_int, _D, _I]),
     "cns_ctoprim": (C.c_int, [_I, _I, _D, _D, _D, C.c_int, _D]),
     "cns_hypterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, _D]),
     "cns_diffterm": (C.c_int, [_I, _I, C.c_int, _D, _D, _D, C.c_double, C.c_double]),

@@ -59,6 +59,12 @@ extern "C" int cns_selftest_bounded_wait(int* status) {
     CK(bounded_wait_selftest(status));
     return CNS_OK;
 }
+extern "C" int cns_selftest_exact_sums(const double* taps, int n, double* sums, int* ok) {
+    if (!taps || !sums || !ok) return fail(CNS_ERR_INVALID, "null argument");
+    if (n < 0 || n > (1 << 24)) return fail(CNS_ERR_INVALID, "n=%d outside 0..2^24", n);
+    CK(exact_sums_selftest(taps, n, sums, ok));
+    return CNS_OK;
+}
 
 extern "C" int cns_measure_fp64_peak(double* tflops) {
     if (!tflops) return fail(CNS_ERR_INVALID, "null argument");

@@ -39,6 +39,7 @@ void tma_tile_shape(int* ti, int* tj, int* tk);
 size_t tma_maps_bytes();
 cudaError_t tma_encode_maps(const BoxView& v, void* out);
 cudaError_t bounded_wait_selftest(int* status);
+cudaError_t exact_sums_selftest(const double* taps, int n, double* sums, int* ok);
 cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 cudaError_t launch_assemble_tma64(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 // the mixed form's derivative pass on the same tiles, TMA-staged (same bits as launch_deriv)

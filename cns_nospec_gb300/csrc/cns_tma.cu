@@ -890,6 +890,44 @@ cudaError_t bounded_wait_selftest(int* status) {
     return e;
 }
 
+// Self-test of the exact stencil sums (cns_exact.cuh) as the device computes them: set q has the
+// taps taps[8q .. 8q+7] = f[+1..+4], f[-1..-4]; sums[2q] and sums[2q+1] get the sums with the
+// first- and the second-derivative weights, ok[2q] and ok[2q+1] are 0 where a sum takes the
+// FP64 fallback instead.
+__global__ void k_exact_sums_selftest(const double* __restrict__ taps, int n, double* __restrict__ sums,
+                                      int* __restrict__ ok) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const double* t = taps + 8LL * q;
+        auto ld = [&](int m) { return m > 0 ? t[m - 1] : t[3 - m]; };  // m = 1..4, -1..-4
+        double x1 = 0.0, x2 = 0.0;
+        ok[2 * q] = xsum8<672, -168, 32, -3, -1>(ld, &x1) ? 1 : 0;
+        ok[2 * q + 1] = xsum8<8064, -1008, 128, -9, 1>(ld, &x2) ? 1 : 0;
+        sums[2 * q] = x1;
+        sums[2 * q + 1] = x2;
+    }
+}
+
+cudaError_t exact_sums_selftest(const double* taps, int n, double* sums, int* ok) {
+    if (n <= 0) return cudaSuccess;
+    double *dt = nullptr, *ds = nullptr;
+    int* dk = nullptr;
+    cudaError_t e = cudaMalloc(&dt, sizeof(double) * 8 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&ds, sizeof(double) * 2 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&dk, sizeof(int) * 2 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(dt, taps, sizeof(double) * 8 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const int grid = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+        k_exact_sums_selftest<<<grid, 256>>>(dt, n, ds, dk);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(sums, ds, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ok, dk, sizeof(int) * 2 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(dt);
+    cudaFree(ds);
+    cudaFree(dk);
+    return e;
+}
+
 // ---- host side -------------------------------------------------------------------------------
 constexpr size_t kTmaSmem = 2 * kBufElems * sizeof(float) + 2 * sizeof(uint64_t);
 

@@ -80,6 +80,12 @@ int cns_measure_fp64_peak(double *tflops);
  * reports *status = CNS_HEALTH_TIMEOUT (8) instead of hanging.  No counterpart in the
  * reference. */
 int cns_selftest_bounded_wait(int *status);
+/* Self-test of the exact 8-tap stencil sums of the plain form as the device computes them:
+ * for n sets of taps (taps[8q..8q+7] = f[+1..+4], f[-1..-4]) writes the sums with the
+ * first-derivative weights (672, -168, 32, -3) to sums[2q] and with the second-derivative
+ * weights (8064, -1008, 128, -9) to sums[2q+1], and ok[2q], ok[2q+1] = 0 where a sum takes the
+ * FP64 fallback.  Host arrays; n <= 2^24.  No counterpart in the reference. */
+int cns_selftest_exact_sums(const double *taps, int n, double *sums, int *ok);
 
 /* ---- operator level: the reference's per-operator surface, host arrays ---------------- */
 
