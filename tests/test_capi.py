@@ -63,6 +63,11 @@ def test_invalid_arguments_are_rejected_before_any_device_work(cns):
     assert lib.cns_ctoprim(lo, hi, None, None, L.darr([1, 1, 1]), 4, None) == L.CNS_ERR_INVALID
     assert lib.cns_ctoprim(lo, hi, None, None, L.darr([1, 1, 1]), 2, None) == L.CNS_ERR_INVALID
     assert lib.cns_box_advance(None, 1) == L.CNS_ERR_INVALID
+    taps, sums, ok = (ctypes.c_double * 8)(*([1.0] * 8)), (ctypes.c_double * 2)(), (ctypes.c_int * 2)()
+    assert lib.cns_selftest_exact_sums(None, 1, sums, ok) == L.CNS_ERR_INVALID
+    assert lib.cns_selftest_exact_sums(taps, -1, sums, ok) == L.CNS_ERR_INVALID
+    assert lib.cns_selftest_exact_sums(taps, 1 << 25, sums, ok) == L.CNS_ERR_INVALID
+    assert lib.cns_selftest_exact_sums(taps, 0, sums, ok) == 0  # nothing to do, no device work
 
 
 def test_box_bytes_accounts_for_state_and_stencil_sets(cns):
