@@ -6,13 +6,17 @@
 //   first derivative  (ALP, BET, GAM, DEL)     = ( 672, -168,  32, -3) / 840
 //   second derivative (OFF1, OFF2, OFF3, OFF4) = (8064, -1008, 128, -9) / 5040
 // (cpu/header.h:88-91, cpu/diffterm.cpp:48-52), so sum_m w_m (f[+m] -+ f[-m]) can be formed
-// exactly in integers: each tap's 53-bit significand is placed 9 bits below the ulp of the
-// largest tap (a tap more than 9 binades smaller keeps its bits down to 2^-62 of the largest
-// one), split into two 31-bit halves, multiplied by its signed weight and summed in two 64-bit
-// accumulators (one wide multiply-add per half), then rounded once to FP64, to nearest even.
+// in integers: each tap's 53-bit significand is placed 9 bits below the ulp of the largest tap
+// (the bits of a tap that lie below 2^-62 of the largest one are truncated), split into two
+// 31-bit halves, multiplied by its signed weight and summed in two 64-bit accumulators (one
+// wide multiply-add per half) without any rounding, then rounded once to FP64, to nearest even.
+// The result is therefore within half an ulp of itself plus sum|w| * 2^(emax - 1084) of the
+// true sum (emax the largest tap's biased exponent field): a few ulp of the largest tap.  Where
+// the taps lie within 9 binades of one another nothing is truncated and the result is the
+// correctly rounded sum; where the largest taps cancel (f[+1] = f[-1] in a first derivative)
+// the truncation can leave fewer good bits than the FP64 chain, whose f[+1] - f[-1] is exact.
 // The caller scales the sum by its per-axis factor (coefficient / 840 or / 5040) in one FP64
-// FMA: one FP64 instruction per stencil instead of eight, and a sum that is correctly rounded
-// where the FP64 chain rounds eight times.  Taps that are not finite, and nonzero sums outside
+// FMA: one FP64 instruction per stencil instead of eight.  Taps that are not finite, and nonzero sums outside
 // FP64's normal range (|sum| below 2^-1022 or at least 2^1023), report failure; the caller then
 // takes the FP64 chain, so every input gives what FP64 arithmetic gives.
 #pragma once

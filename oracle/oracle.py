@@ -21,7 +21,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libcns_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libcnsref.so")
-REF_SRC = "/root/reference/cpu"
+# Where the reference tree lies (its cpu/ sources are compiled unmodified by the Makefile's
+# `ref` target); CNS_REFERENCE_DIR overrides it.  Absent on machines without the tree.
+REF_ROOT = os.environ.get("CNS_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "cpu")
 
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)

@@ -91,7 +91,8 @@ def test_global_const_layout_matches_reference_struct():
 
 
 def test_global_const_layout_against_reference_header(tmp_path):
-    hdr = "/root/reference/cpu/header.h"
+    from oracle import oracle as O
+    hdr = os.path.join(O.REF_SRC, "header.h")
     if not os.path.exists(hdr):
         pytest.skip("reference tree not present")
     src = tmp_path / "probe.cpp"
@@ -101,6 +102,6 @@ def test_global_const_layout_against_reference_header(tmp_path):
         ' offsetof(global_const_t, OFF4), offsetof(cns_global_const_t, OFF4));}\n' % os.path.join(ROOT, "include",
                                                                                                  "cns_gb300.h"))
     exe = tmp_path / "probe"
-    subprocess.run(["g++", "-I/root/reference/cpu", str(src), "-o", str(exe)], check=True)
+    subprocess.run(["g++", "-I" + O.REF_SRC, str(src), "-o", str(exe)], check=True)
     a, b, c, d = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert a == b and c == d

@@ -14,7 +14,7 @@ from conftest import FP64_TOL, ROOT, golden, normwise
 
 DROPIN = os.path.join(ROOT, "cns_nospec_gb300", "dropin", "advance_gb300.cpp")
 LIBDIR = os.path.join(ROOT, "cns_nospec_gb300")
-REF = "/root/reference/cpu"
+from oracle.oracle import REF_SRC as REF  # noqa: E402
 
 
 def _build_driver(tmp, header_dir):

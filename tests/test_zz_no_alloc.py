@@ -1,9 +1,11 @@
 """cns_diffterm_noalloc: diffterm for callers that cannot allocate device memory while they run
 (their device memory belongs to another allocator or a fixed budget, or they cannot afford
 cudaMalloc's synchronisation).  It takes caller-owned device buffers and keeps its
-temporaries in one fixed device array.  Checked through the C ABI against cns_diffterm on
-two calls in a row (the second call finds the first call's data in the shared array), with
-the normwise tolerance of the other FP64 parity tests.  Collected last on purpose."""
+temporaries in one fixed device array.  Checked through the C ABI on two calls in a row (the
+second call finds the first call's data in the shared array): the first against the golden D
+the reference's own diffterm produced (tests/golden/ops_6x9x11.npz), the second against the
+oracle's diffterm on another box, with the normwise tolerance of the other FP64 parity tests.
+Collected last on purpose."""
 import ctypes
 
 import numpy as np
@@ -28,25 +30,18 @@ def _noalloc(lib, L, torch, Q, dx, eta, alam):
     return d_dev.cpu().numpy()
 
 
-def _host(cns, Q, dx, eta, alam):
-    n = [Q.shape[a] - 8 for a in range(3)]
-    D = np.zeros(tuple(n) + (5,))
-    cns.diffterm([4, 4, 4], [x + 3 for x in n], 4, dx, np.ascontiguousarray(Q), D, eta, alam)
-    return D
-
-
-def test_diffterm_noalloc_matches_diffterm_twice(gpu, cns):
+def test_diffterm_noalloc_matches_reference_twice(gpu, cns, oracle):
     torch = pytest.importorskip("torch")
     from cns_nospec_gb300 import _lib as L
     lib = cns.load()
     g = golden("ops_6x9x11.npz")
-    first = (g["Q"], tuple(g["dx"]), float(g["eta"]), float(g["alam"]))
+    first = (g["Q"], tuple(g["dx"]), float(g["eta"]), float(g["alam"]), g["D"])
     n2 = (12, 10, 8)
-    Q2, _ = cns_ctoprim_host(cns, I.initial_state(n2, perturb=1e-3, seed=31), I.box_dx(n2))
-    second = (Q2, I.box_dx(n2), I.ETA * 1.1, I.ALAM * 0.9)
-    for Q, dx, eta, alam in (first, second):
+    Q2, _ = oracle.ctoprim(I.initial_state(n2, perturb=1e-3, seed=31), I.box_dx(n2))
+    eta2, alam2 = I.ETA * 1.1, I.ALAM * 0.9
+    second = (Q2, I.box_dx(n2), eta2, alam2, oracle.diffterm(Q2, I.box_dx(n2), eta2, alam2))
+    for Q, dx, eta, alam, want in (first, second):
         got = _noalloc(lib, L, torch, Q, dx, eta, alam)
-        want = _host(cns, Q, dx, eta, alam)
         assert np.all(np.isfinite(got))
         assert normwise(got, want, interior_only=False).max() <= FP64_TOL
 
@@ -59,10 +54,3 @@ def test_diffterm_noalloc_rejects_boxes_above_its_limit(gpu, cns):
                                   ctypes.c_void_p(16), ctypes.c_void_p(16), 1e-4, 100.0, None)
     assert rc == L.CNS_ERR_CAPACITY
     assert b"64000" in lib.cns_last_error()
-
-
-def cns_ctoprim_host(cns, U, dx):
-    n = [U.shape[a] - 8 for a in range(3)]
-    Q = np.zeros(U.shape[:3] + (6,))
-    c = cns.ctoprim([4, 4, 4], [x + 3 for x in n], U, Q, dx, 4, courno=1e-50)
-    return Q, c
