@@ -1,9 +1,12 @@
 """Benchmark: cell-updates/s of the RK3 advance on one periodic box.
 
-Workload (default): 128^3 cells + 4 ghost cells a side, FP64 plain form, the CNS_NoSpec
-initial field with a seeded +-1e-3 perturbation of rho, u, v, w; a step is one full RK3
-step (new_advance, cpu/advance.cpp:13-154) of that box.  The mixed FP32/FP64 form is timed on
-the same box in the same run and its error against the FP64 result is reported.
+Workload (default): 256^3 cells + 4 ghost cells a side, the CNS_NoSpec initial field with a
+seeded +-1e-3 perturbation of rho, u, v, w; a step is one full RK3 step (new_advance,
+cpu/advance.cpp:13-154) of that box.  `value` is the plain FP64 form, device-resident and
+graph-replayed; the same line carries the mixed FP32/FP64 form on the same box (its rate and its
+error against the FP64 form after 100 steps), the end-to-end rate through the reference-facing
+call with page-locked and with pageable host arrays, the 128^3 box, a batch of 256 uneven boxes
+and a short serving stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -27,36 +30,37 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Algorithmic FP64 work of one cell-update (one cell, one full RK3 step) in the reference's
-# formulation (each +, -, *, / one flop): 3 x (ctoprim 16 + hypterm 358 + diffterm 415)
-# + RK combines 15 + 30 + 30 + Courant 8 = 2450.
+# The reference's FP64 operation count of one cell-update (one cell, one full RK3 step; each
+# +, -, *, / one flop): 3 x (ctoprim 16 + hypterm 358 + diffterm 415) + RK combines 15 + 30 + 30
+# + Courant 8 = 2450.  Reported as a reference-op throughput; the roofline uses the FP64
+# operations the kernels execute (counted by ncu).
 FLOPS_PER_CELL_UPDATE = 2450
-# Of that, per cell and launch: k_deriv does the nine first derivatives (9 x 12) and the
-# dissipation terms of diffterm's energy component (24) = 132; k_assemble the rest of a stage.
-FLOPS_DERIV = 132
-FLOPS_ASSEMBLE_PER_STEP = FLOPS_PER_CELL_UPDATE - 3 * FLOPS_DERIV  # 2054 over 3 launches
 # Compulsory HBM traffic of one cell-update with the FP64 state: stage 1 reads U^n and writes
 # U^1 (80 B); stages 2 and 3 read U^(k), U^n and write U^(k+1) (120 B each).
 BYTES_PER_CELL_UPDATE = 320
+MIXED_ERROR_STEPS = 100
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--size", dest="n", type=int, default=128, help="cells per axis of the periodic box")
+    p.add_argument("--size", dest="n", type=int, default=256, help="cells per axis of the periodic box")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
-    p.add_argument("--case", choices=["fp64", "mixed", "e2e"], default=None,
+    p.add_argument("--no-extras", action="store_true",
+                   help="only the headline box (no 128^3 box, batch, serving stream or pageable e2e)")
+    p.add_argument("--cpu-seconds", type=float, default=16.0, help="CPU baseline sample length (timed part)")
+    p.add_argument("--case", choices=["fp64", "mixed", "e2e", "e2e_pageable"], default=None,
                    help="profiling case: only upload + warmup + steps of one form (for ncu), then exit; "
-                        "e2e: warmup + steps calls of cns_new_advance on a page-locked host array")
+                        "e2e: warmup + steps calls of cns_new_advance on a page-locked host array "
+                        "(e2e_pageable: on a pageable one)")
     p.add_argument("--kernel", choices=["ws", "tma", "direct"], default=None,
                    help="--case: the assembly kernel (default: the library's choice; ws is mixed-only)")
     p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve", "cpu"], default="box",
-                   help="box: the headline 128^3 line (default); batch: 256 uneven boxes; "
-                        "mixed256: FP64 vs mixed at --size (use 256); serve: the request stream; "
+                   help="box: the headline line (default); batch: 256 uneven boxes; "
+                        "mixed256: FP64 vs mixed at --size; serve: the request stream; "
                         "cpu: the CPU baseline table (the oracle port on the host cores)")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     p.add_argument("--boxes", type=int, default=256)
@@ -150,6 +154,15 @@ def box_workload(n):
     return f"periodic box {n}^3 + 4 ghosts, FP64 RK3 step, sinusoidal field with a 1e-3 perturbation (seed 1)"
 
 
+def workload_config(n):
+    """`config` of the JSON line: identical on both arms (the arms' own details go elsewhere)."""
+    # the FP64 box's device state: U, the stage state, two 16-field primitive/flux sets and the
+    # 4-field derivative set, 46 doubles per ghost-inclusive cell
+    big = 46 * 8 * (n + 8) ** 3 > 129e6
+    return {"workload": box_workload(n), "n": n, "steps_per_call": 1,
+            "l2": "inputs larger than L2 (no flush)" if big else "inputs smaller than L2 (resident between steps)"}
+
+
 def pinned_like(shape):
     """A pinned host float64 array when torch is importable (plumbing only), else pageable."""
     try:
@@ -160,16 +173,13 @@ def pinned_like(shape):
         return np.empty(shape, dtype=np.float64), False, None
 
 
-def measured_traffic(kernel: str, n: int):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, scaled by cells."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+def profile_json(name: str):
+    """A committed ncu summary in machine-readable form (profiles/<name>.json), or {}."""
     try:
-        with open(path) as f:
-            t = json.load(f)
-        per_cell = t[kernel]["dram_bytes_per_cell"]
-        return per_cell * n ** 3, t[kernel].get("source")
-    except Exception:
-        return None, None
+        with open(os.path.join(ROOT, "profiles", name + ".json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 # ---- CPU baseline: the oracle (the reference's algorithm restated in C) on the host cores ----
@@ -195,41 +205,26 @@ def cpu_model() -> str:
 
 def cpu_baseline(n: int, seconds: float):
     """The reference algorithm (the oracle port, the reference's cpu/ operation order) on the
-    host cores: one single-threaded process per core, each advancing its own n^3 box, for about
-    `seconds` (oracle_processes); beside it one core alone at 32^3 and n^3, and all cores as one
-    OpenMP process on one box."""
+    host cores: one single-threaded process per core, each advancing its own n^3 box (one
+    untimed step, then about `seconds` of timed steps; oracle_processes); beside it one core
+    alone at 32^3."""
     from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
     O.build(ref=os.path.isdir(O.REF_SRC))
-    cores = os.cpu_count() or 1
     nproc = host_processes(n)
-    value, steps, wall = oracle_processes(n, 100, 1, seconds, nproc)
-    # one core, as the reference's own cpu/ path runs (its OpenMP pragmas are commented out)
-    one = {}
+    value, steps, wall = oracle_processes(n, 1000, 1, seconds, nproc)
     O.set_threads(1)
-    for m, budget in ((32, 1.0), (n, 3.0)):
-        V = I.initial_state(m, perturb=1e-3, seed=1)
-        k, t1 = 0, time.perf_counter()
-        while True:
-            V, _ = O.advance(V, 1, I.box_dx(m), I.CFL, I.ETA, I.ALAM, which="port")
-            k += 1
-            e1 = time.perf_counter() - t1
-            if e1 >= budget or k >= 50:
-                break
-        one[str(m)] = m ** 3 * k / e1
-    threads = O.set_threads(cores)
-    U = I.initial_state(n, perturb=1e-3, seed=1)
+    V = I.initial_state(32, perturb=1e-3, seed=1)
     k, t1 = 0, time.perf_counter()
     while True:
-        U, _ = O.advance(U, 1, I.box_dx(n), I.CFL, I.ETA, I.ALAM, which="port")
+        V, _ = O.advance(V, 1, I.box_dx(32), I.CFL, I.ETA, I.ALAM, which="port")
         k += 1
         e1 = time.perf_counter() - t1
-        if e1 >= 4.0 or k >= 20:
+        if e1 >= 1.0 or k >= 50:
             break
     return {"value": value, "unit": "cell-updates/s", "cores": nproc, "cpu_model": cpu_model(), "kind": "port",
             "sample": f"{nproc} single-threaded processes, {steps} RK3 steps in all of their own {n}^3 boxes, "
-                      f"{wall:.1f} s", "one_core_by_n": one,
-            "openmp_one_process": {"value": n ** 3 * k / e1, "threads": threads, "steps": k}}
+                      f"{wall:.1f} s", "one_core_32": 32 ** 3 * k / e1}
 
 
 def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
@@ -243,7 +238,7 @@ def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
     dx = I.box_dx(n)
     for _ in range(warmup):
         U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
-    barrier.wait(timeout=600)
+    barrier.wait(timeout=900)
     k, t0 = 0, time.time()
     while k < steps:
         U, _ = O.advance(U, 1, dx, I.CFL, I.ETA, I.ALAM, which=which)
@@ -254,37 +249,38 @@ def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
 
 
 def host_processes(n: int) -> int:
-    """Processes for oracle_processes: one per host core, but no more than a quarter of the
-    host's memory holds (an n^3 oracle step needs about 25 doubles per ghost-inclusive cell)."""
+    """Processes for oracle_processes: one per host core, but no more than half of the host's
+    memory holds (an n^3 oracle step holds about 34 doubles per ghost-inclusive cell: U, Unew,
+    Q, D, F and diffterm's nine temporaries)."""
     cores = os.cpu_count() or 1
     try:
         mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
     except (ValueError, OSError, AttributeError):
         return cores
-    per = 25 * 8 * (n + 8) ** 3
-    return max(1, min(cores, int(mem // 4 // per)))
+    per = 34 * 8 * (n + 8) ** 3
+    return max(1, min(cores, int(mem // 2 // per)))
 
 
 def oracle_processes(n, steps, warmup, seconds, nproc, which="port"):
     """The reference algorithm on every host core the way its single-threaded cpu/ code uses
     them: `nproc` independent processes (spawned), each advancing its own copy of the n^3 box,
     their timed parts started together.  Throughput = all processes' cell-updates / (last end -
-    first start)."""
+    first start).  Returns (throughput, steps done in all, wall seconds)."""
     import multiprocessing as mp
+    import queue
     ctx = mp.get_context("spawn")
     barrier, out = ctx.Barrier(nproc), ctx.Queue()
     procs = [ctx.Process(target=_oracle_process, args=(n, steps, warmup, seconds, which, barrier, out))
              for _ in range(nproc)]
     for p in procs:
         p.start()
-    import queue
     res, t0 = [], time.time()
     try:
         while len(res) < nproc:
             try:
                 res.append(out.get(timeout=5))
             except queue.Empty:
-                if any(p.exitcode not in (None, 0) for p in procs) or time.time() - t0 > 900:
+                if any(p.exitcode not in (None, 0) for p in procs) or time.time() - t0 > 1800:
                     raise RuntimeError("an oracle process failed or did not finish")
     finally:
         for p in procs:
@@ -327,12 +323,13 @@ def run_cpu_table(args):
 
 
 def run_reference(args, dist):
-    """--impl reference: the reference algorithm on the host cores, same workload.  Where the
-    reference tree exists its own cpu/ objects run (oracle/_ref); elsewhere (the GPU machine, where
-    it is absent and x86 objects do not travel) the oracle port, which gives the same bits.
-    Its cpu/ path is single-threaded, so it uses the cores as one process per core, each
-    advancing its own copy of the box (oracle_processes): `warmup` untimed steps, then `steps`
-    timed steps, bounded to about a minute."""
+    """--impl reference: the reference algorithm on the host cores, on the same workload, with
+    the same warm-up and timed step counts as the GPU arm.  Where the reference tree exists its
+    own cpu/ objects run (oracle/_ref); elsewhere (where it is absent and x86 objects do not
+    travel) the oracle port, which gives the same bits.  Its cpu/ path is single-threaded, so it
+    uses the cores as one process per core, each advancing its own copy of the box
+    (oracle_processes): `warmup` untimed steps each, then `steps` timed steps each (a step of
+    this arm: every process advances its box one RK3 step), bounded to 20 minutes."""
     if dist.rank != 0:
         return None
     from oracle import oracle as O
@@ -340,19 +337,110 @@ def run_reference(args, dist):
     use_ref = O.have_ref() and os.path.isdir(O.REF_SRC)
     which = "ref" if use_ref else "port"
     n = args.n
-    cores = host_processes(n)
-    warm = min(args.warmup, 1)
-    v, done, wall = oracle_processes(n, args.steps, warm, 60.0, cores, which=which)
-    steps = max(1, done // cores)
+    procs = host_processes(n)
+    v, done, wall = oracle_processes(n, args.steps, args.warmup, 1200.0, procs, which=which)
+    steps = max(1, done // procs)
     kind = "reference" if use_ref else "port"
-    sample = f"{cores} single-threaded processes x {steps} RK3 steps of their own {n}^3 box, {wall:.1f} s"
+    sample = (f"{procs} single-threaded processes x ({args.warmup} untimed + {steps} timed) RK3 steps of their own "
+              f"{n}^3 box, {wall:.1f} s timed")
     return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * wall / steps, "higher_is_better": True,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": box_workload(n), "n": n, "host_processes": cores},
-            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "cpu_model": cpu_model(), "kind": kind,
+            "config": workload_config(n),
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": procs, "cpu_model": cpu_model(), "kind": kind,
                              "sample": sample},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def time_box(C, n, prec, warmup, steps, sampler=None):
+    """One n^3 box of the perturbed field in form `prec`: autotuned (state restored), `warmup`
+    steps, then `steps` graph-replayed steps timed with CUDA events on the box's stream (under
+    `sampler`, the clock sampler, when given), then the same number of steps again through the
+    event-per-kernel path for the kernel split.  Returns a dict."""
+    from cns_nospec_gb300 import initdata as I
+    box = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
+    box.init_field((1.0, 1.0, 1.0), 1e-3, 1)
+    tile, kern, _ = box.autotune(trial_steps=2)
+    box.advance(warmup)
+    box.sync()
+    if sampler is not None:
+        with sampler:
+            ms = box.advance_ms(steps)
+    else:
+        ms = box.advance_ms(steps)
+    kms, klaunch, _ = box.advance_timed(steps)
+    box.sync()
+    launches = box.launches_per_step() * steps
+    box.close()
+    return {"ms": ms, "value": n ** 3 * steps / (ms * 1e-3), "tile": tile, "kernel": kern, "kernel_ms": kms,
+            "kernel_launches": klaunch, "launches": launches}
+
+
+def mixed_error(C, n, steps):
+    """Normwise max and RMS error per conserved variable of the mixed form against the FP64 form
+    after `steps` RK3 steps from the same device-generated state."""
+    from cns_nospec_gb300 import initdata as I
+    ends = {}
+    for prec in (C.CNS_FP64, C.CNS_MIXED):
+        b = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
+        b.init_field((1.0, 1.0, 1.0), 1e-3, 1)
+        b.advance(steps)
+        b.sync()
+        ends[prec] = b.download()
+        b.close()
+    mx, rms = I.normwise_error(ends[C.CNS_MIXED], ends[C.CNS_FP64])
+    return {"steps": steps, "vars": ["rho", "rho u", "rho v", "rho w", "rho E"],
+            "max": [float(x) for x in mx], "rms": [float(x) for x in rms], "worst": float(mx.max())}
+
+
+def time_e2e(C, lib, n, U0, Uh, calls, dist):
+    """cns_new_advance (the reference's new_advance) on the host array Uh, one RK3 step per call,
+    `calls` calls timed on the host clock with a device synchronize on both sides: the upload of
+    U, the step and the download of U each call.  Returns (cell-updates/s, ms per call)."""
+    from cns_nospec_gb300 import initdata as I
+    h = C.read_configurations(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    Uh[...] = U0
+    C.new_advance(Uh, None, None, None, None, h)  # warm (creates the cached device state)
+    Uh[...] = U0
+    lib.cns_device_synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        C.new_advance(Uh, None, None, None, None, h)
+    lib.cns_device_synchronize()
+    el = dist.max(time.perf_counter() - t0)
+    dist.barrier()
+    return dist.world * n ** 3 * calls / el, 1e3 * el / calls
+
+
+def fp64_roofline(kernel_ms, klaunch, names, cells, fp64_peak):
+    """The roofline of the FP64 form's dominant kernel: the FP64 operations it executes per cell
+    (ncu's DFMA, DADD and DMUL thread-instruction counts, a DFMA counting 2) over its live launch
+    time, against the FP64 FMA rate this process measured.  The per-cell counts and DRAM bytes come
+    from the committed capture (profiles/fp64_counters.json; per cell, so they scale to any box)."""
+    dom = int(np.argmax(kernel_ms))
+    name = names[dom]
+    launch_ms = kernel_ms[dom] / max(klaunch[dom], 1)
+    cnt = profile_json("fp64_counters").get(name, {})
+    out = {"bound": "fp64", "kernel": name, "launch_ms": launch_ms, "peak": fp64_peak, "unit": "TFLOP/s",
+           "peak_source": "measured live: FP64 FMA probe kernel (cns_measure_fp64_peak)"}
+    if "fp64_flops_per_cell" in cnt:
+        flops = cnt["fp64_flops_per_cell"] * cells
+        inst = cnt["fp64_inst_per_cell"] * cells
+        achieved = flops / (launch_ms * 1e-3) / 1e12
+        # the probe's DFMA rate in warp-lane instructions per second is fp64_peak / 2
+        out.update({"achieved": achieved, "frac": achieved / fp64_peak, "flops_per_launch": flops,
+                    "fp64_inst_rate_frac": inst / (launch_ms * 1e-3) / (fp64_peak * 1e12 / 2),
+                    "basis": "FP64 operations executed, counted by ncu per cell (DFMA = 2, DADD and DMUL = 1)",
+                    "fp64_pipe_active_ncu": cnt.get("fp64_pipe_active"),
+                    "alu_pipe_active_ncu": cnt.get("alu_pipe_active"),
+                    "issue_active_ncu": cnt.get("issue_active"),
+                    "counters": "fp64_counters.json: " + name})
+    else:
+        out.update({"achieved": None, "frac": None, "counters": None})
+    tr = cnt.get("dram_bytes_per_cell")
+    out["traffic"] = tr * cells if tr is not None else None
+    return out
 
 
 def run_ours(args, dist):
@@ -363,144 +451,106 @@ def run_ours(args, dist):
     B.build()
     lib = C.load()
     L.check(lib.cns_set_device(dist.local))
-    n = args.n
-    dx = I.box_dx(n)
-    U0 = I.initial_state(n, perturb=1e-3, seed=1)
-
-    fp64_peak = C._lib.C.c_double(0.0)
-    L.check(lib.cns_measure_fp64_peak(C._lib.C.byref(fp64_peak)))
+    n, cells = args.n, args.n ** 3
+    names = L.KERNEL_NAMES
+    fp64_peak = ctypes.c_double(0.0)
+    L.check(lib.cns_measure_fp64_peak(ctypes.byref(fp64_peak)))
     fp64_peak = fp64_peak.value
 
-    # ---- device-resident FP64 plain form: the headline value --------------------------------
-    box = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_FP64)
-    box.upload(U0)
-    tile64, _, _ = box.autotune(trial_steps=2)  # state restored afterwards
-    box.advance_timed(args.warmup)
-    lib.cns_device_synchronize()
+    # ---- the headline: device-resident FP64 plain form, graph-replayed --------------------
     dist.barrier()
-    with ClockSampler(dist.local) as clk:
-        lib.cns_device_synchronize()
-        kms, klaunch, total_ms = box.advance_timed(args.steps)
-        lib.cns_device_synchronize()
+    clk = ClockSampler(dist.local)
+    f64 = time_box(C, n, C.CNS_FP64, args.warmup, args.steps, sampler=clk)
+    t_max = dist.max(f64["ms"])
     dist.barrier()
-    box.sync()
-    t_max = dist.max(total_ms)
-    cells = n ** 3
     value = dist.world * cells * args.steps / (t_max * 1e-3)
-    U64 = box.download()
-    box.close()
+    step_ms = t_max / args.steps
 
-    # ---- mixed form on the same box ----------------------------------------------------------
-    mbox = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=C.CNS_MIXED)
-    mbox.upload(U0)
-    tile32, kern32, _ = mbox.autotune(trial_steps=2)
-    mbox.advance_timed(args.warmup)
-    mms, _, mtotal = mbox.advance_timed(args.steps)
-    mbox.sync()
-    mbox.close()
-    mixed_value = cells * args.steps / (mtotal * 1e-3)
-    # error of the mixed form against FP64 after exactly 100 RK3 steps from the same state
-    ends = {}
-    for prec in (C.CNS_FP64, C.CNS_MIXED):
-        eb = C.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=prec)
-        eb.upload(U0)
-        eb.advance(100)
-        eb.sync()
-        ends[prec] = eb.download()
-        eb.close()
-    mixed_err = I.normwise_error(ends[C.CNS_MIXED], ends[C.CNS_FP64])[0]
-    del U64
+    # ---- mixed form on the same box, and its error after 100 steps ----------------------
+    mix = time_box(C, n, C.CNS_MIXED, args.warmup, args.steps)
+    err = mixed_error(C, n, MIXED_ERROR_STEPS)
 
-    # ---- end to end through the reference-facing C ABI: host buffers, copies timed ----------
-    h = C.read_configurations(n, dx, I.CFL, I.ETA, I.ALAM)
+    # ---- end to end through the reference-facing call, host arrays ----------------------
+    b0 = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    b0.init_field((1.0, 1.0, 1.0), 1e-3, 1)
+    U0 = b0.download()
+    b0.close()
+    calls = max(1, min(args.steps, 20))
     Uh, pinned, _keep = pinned_like(U0.shape)
-    Uh[...] = U0
-    k_e2e = max(1, min(args.steps, 20))
-    C.new_advance(Uh, None, None, None, None, h)  # warm (allocates the cached device state)
-    Uh[...] = U0
-    lib.cns_device_synchronize()
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(k_e2e):
-        C.new_advance(Uh, None, None, None, None, h)
-    lib.cns_device_synchronize()
-    e2e_s = dist.max(time.perf_counter() - t0)
-    dist.barrier()
-    e2e_value = dist.world * cells * k_e2e / e2e_s
-    # bytes that cross the CPU-GPU link per call: in place (page-locked U) the interior goes in and
-    # the interior plus the ghost images come out; staged, the whole array both ways
+    e2e_value, e2e_ms = time_e2e(C, lib, n, U0, Uh, calls, dist)
     flag = ctypes.c_int(0)
     L.check(lib.cns_host_in_place(ctypes.c_void_p(Uh.ctypes.data), ctypes.c_longlong(Uh.nbytes), ctypes.byref(flag)))
     in_place = bool(flag.value)
-    h2d_bytes = n ** 3 * 5 * 8 if in_place else int(Uh.nbytes)
-    d2h_bytes = int(Uh.nbytes)
+    e2e = {"value": e2e_value, "unit": "cell-updates/s",
+           "h2d_bytes_per_step": cells * 5 * 8 if in_place else int(Uh.nbytes), "d2h_bytes_per_step": int(Uh.nbytes),
+           "ms_per_call": e2e_ms, "calls": calls, "pinned_host": pinned, "in_place": in_place,
+           "api": "cns_new_advance (host U in, 1 RK3 step, U out)"}
+    del Uh, _keep
+    extras = {}
+    if not args.no_extras and dist.world == 1:
+        Up = np.array(U0)  # pageable, as the reference's malloc'd arrays are
+        pv, pms = time_e2e(C, lib, n, U0, Up, calls, dist)
+        L.check(lib.cns_host_in_place(ctypes.c_void_p(Up.ctypes.data), ctypes.c_longlong(Up.nbytes),
+                                      ctypes.byref(flag)))
+        extras["e2e_pageable"] = {"value": pv, "unit": "cell-updates/s", "ms_per_call": pms, "calls": calls,
+                                  "in_place": bool(flag.value), "vs_pinned_e2e": pv / e2e_value,
+                                  "h2d_bytes_per_step": cells * 5 * 8 if flag.value else int(Up.nbytes),
+                                  "d2h_bytes_per_step": int(Up.nbytes),
+                                  "api": "cns_new_advance on a pageable (malloc'd) host array"}
+        del Up
+    del U0
 
-    # ---- roofline of the dominant kernel ----------------------------------------------------
-    names = L.KERNEL_NAMES
-    dom = int(np.argmax(kms))
-    dom_launch_ms = kms[dom] / max(klaunch[dom], 1)
-    if names[dom] == "k_assemble":
-        flops_launch = FLOPS_ASSEMBLE_PER_STEP / 3.0 * cells
-    else:
-        flops_launch = FLOPS_DERIV * cells
-    achieved_tf = flops_launch / (dom_launch_ms * 1e-3) / 1e12
-    traffic, tsrc = measured_traffic(names[dom], n)
-    step_ms = t_max / args.steps
+    roof = fp64_roofline(f64["kernel_ms"], f64["kernel_launches"], names, cells, fp64_peak)
     hbm_gbs = BYTES_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e9
-    peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except Exception:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    launches_per_step = sum(klaunch) / args.steps
-
+            hbm_peak = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        hbm_peak = None
+    if hbm_peak is None:
+        hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
+    else:
+        hbm_src = "MEASURED_PEAKS.json hbm_gbs"
+    ksplit = lambda r: {names[i]: r["kernel_ms"][i] / args.steps for i in range(L.KERN_COUNT)}
     result = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": box_workload(n),
-                   "n": n, "form": "fp64 plain", "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
-                   "arithmetic": "FP64; 19 of the 39 8-tap stencil sums per cell and stage formed exactly in "
-                                 "64-bit integers on the significands and rounded once to FP64",
-                   "l2": f"working set {Box_bytes(C, n) / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
-                   "tile_log2_ijk": {"fp64": list(tile64), "mixed": list(tile32)},
-                   "mixed_assembly_kernel": {C.CNS_ASSEMBLE_TMA: "tma", C.CNS_ASSEMBLE_TMA_WS: "tma_ws"}.get(kern32, "direct")},
-        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d_bytes,
-                "d2h_bytes_per_step": d2h_bytes, "in_place": in_place,
-                "api": "cns_new_advance (host U in, 1 RK3 step, U out)",
-                "pinned_host": pinned, "steps": k_e2e},
-        "roofline": {"bound": "fp64", "kernel": names[dom], "achieved": achieved_tf, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak,
-                     "peak_source": "measured live: FP64 FMA probe kernel (cns_measure_fp64_peak)",
-                     "flops_per_launch": flops_launch, "launch_ms": dom_launch_ms,
-                     "flops_basis": "the reference's FP64 operation count (2,450 per cell-update, less k_deriv's "
-                                    "3 x 132, over 3 launches); the fused kernel retires fewer FP64 instructions "
-                                    "than that count, so frac can exceed 1",
-                     "fp64_pipe_busy_ncu": 0.744, "int_pipe_busy_ncu": 0.361,
-                     "pipe_source": "ncu sm__pipe_fp64_cycles_active and sm__inst_executed_pipe_alu of stage 1 "
-                                    "(part of the stencil sums run exactly on the integer pipes), "
-                                    "profiles/k_assemble_fp64_128cube.md",
-                     "traffic": traffic, "traffic_source": tsrc},
+        "config": workload_config(n),
+        "form": {"plain": "FP64; 19 of the 39 8-tap stencil sums per cell and stage formed in 64-bit integers on "
+                          "the significands and rounded once to FP64",
+                 "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
+                 "tile_log2_ijk": {"fp64": list(f64["tile"]), "mixed": list(mix["tile"])},
+                 "mixed_assembly_kernel": {C.CNS_ASSEMBLE_TMA: "tma", C.CNS_ASSEMBLE_TMA_WS: "tma_ws"}.get(
+                     mix["kernel"], "direct"),
+                 "timing": "graph-replayed steps between CUDA events on the box's stream"},
+        "e2e": e2e,
+        "mixed": {"value": mix["value"], "unit": "cell-updates/s", "speedup_vs_fp64": mix["value"] / (value / dist.world),
+                  "error_vs_fp64": err, "steps": args.steps, "kernels_ms_per_step": ksplit(mix)},
+        "roofline": roof,
         "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak, "frac": hbm_gbs / hbm_peak,
-                "bytes_per_cell_update": BYTES_PER_CELL_UPDATE, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-        "fp64_step": {"achieved_tflops": FLOPS_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e12,
-                      "frac_of_fp64_peak": FLOPS_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e12 / fp64_peak},
-        "kernels_ms_per_step": {names[i]: kms[i] / args.steps for i in range(L.KERN_COUNT)},
-        "mixed": {"value": mixed_value, "unit": "cell-updates/s", "speedup_vs_fp64": mixed_value / (value / dist.world),
-                  "max_normwise_err_vs_fp64_after_100_steps": float(mixed_err.max()),
-                  "err_per_var": [float(x) for x in mixed_err], "steps": args.steps,
-                  "kernels_ms_per_step": {names[i]: mms[i] / args.steps for i in range(L.KERN_COUNT)}},
-        "gpu_launches": int(sum(klaunch)),
-        "launches_per_step": launches_per_step,
+                "bytes_per_cell_update": BYTES_PER_CELL_UPDATE, "peak_source": hbm_src},
+        "reference_op_throughput": {"tflops": FLOPS_PER_CELL_UPDATE * cells / (step_ms * 1e-3) / 1e12,
+                                    "basis": "the reference's FP64 operation count, 2,450 per cell-update"},
+        "kernels_ms_per_step": ksplit(f64),
+        "gpu_launches": f64["launches"],
+        "launches_per_step": f64["launches"] / args.steps,
         "clocks": clk.summary(),
     }
+    result.update(extras)
+    if not args.no_extras and dist.world == 1:
+        result["box_128"] = run_box128(C, args)
+        result["batch"] = run_batch_short(C, args)
+        result["serve"] = run_serve_short(C, args)
     return result
 
 
-def Box_bytes(C, n):
-    return C.Box.bytes_for(n, C.CNS_FP64)
+def run_box128(C, args):
+    """The 128^3 box (100-step configuration): both forms' rates and the mixed error."""
+    f = time_box(C, 128, C.CNS_FP64, args.warmup, max(args.steps, 50))
+    m = time_box(C, 128, C.CNS_MIXED, args.warmup, max(args.steps, 50))
+    return {"workload": box_workload(128), "fp64": f["value"], "mixed": m["value"],
+            "speedup": m["value"] / f["value"], "mixed_error_vs_fp64": mixed_error(C, 128, MIXED_ERROR_STEPS)}
 
 
 def run_case(args):
@@ -510,8 +560,11 @@ def run_case(args):
     from cns_nospec_gb300 import initdata as I
     lib = C.load()
     L.check(lib.cns_set_device(0))
-    if args.case == "e2e":
-        Uh, pinned, _keep = pinned_like((args.n + 8,) * 3 + (5,))
+    if args.case in ("e2e", "e2e_pageable"):
+        if args.case == "e2e":
+            Uh, pinned, _keep = pinned_like((args.n + 8,) * 3 + (5,))
+        else:
+            Uh, pinned = np.empty((args.n + 8,) * 3 + (5,)), False
         Uh[...] = I.initial_state(args.n, perturb=1e-3, seed=1)
         h = C.read_configurations(args.n, I.box_dx(args.n), I.CFL, I.ETA, I.ALAM)
         for _ in range(args.warmup):
@@ -521,7 +574,7 @@ def run_case(args):
         for _ in range(args.steps):
             C.new_advance(Uh, None, None, None, None, h)
         lib.cns_device_synchronize()
-        print(json.dumps({"case": "e2e", "n": args.n, "calls": args.steps, "pinned_host": pinned,
+        print(json.dumps({"case": args.case, "n": args.n, "calls": args.steps, "pinned_host": pinned,
                           "ms_per_call": 1e3 * (time.perf_counter() - t0) / max(args.steps, 1)}))
         return
     prec = C.CNS_FP64 if args.case == "fp64" else C.CNS_MIXED
@@ -550,16 +603,13 @@ def batch_specs(count=256, seed=2, nmin=16, nmax=96):
     return out
 
 
-def run_batch(args):
-    """256 uneven boxes (16..96 cells per axis), 50 RK3 steps, one persistent launch per kernel
-    and stage for all boxes, the step captured in a CUDA graph, tile shapes autotuned."""
-    import cns_nospec_gb300 as C
-    from cns_nospec_gb300 import _lib as L
+def batch_run(C, prec, count, steps, warmup, solo=32):
+    """`count` uneven boxes (16..96 cells per axis, seed 2) advanced together: one persistent
+    launch per kernel and stage for all boxes, the step captured in a CUDA graph, the policy
+    (tile shapes, assembly kernel) autotuned; `steps` graph-replayed steps timed with CUDA events.
+    Beside it the first `solo` boxes advanced one at a time (each its own graph)."""
     from cns_nospec_gb300 import initdata as I
-    lib = C.load()
-    L.check(lib.cns_set_device(0))
-    prec = C.CNS_MIXED if args.precision == "mixed" else C.CNS_FP64
-    specs = batch_specs(args.boxes)
+    specs = batch_specs(count)
     boxes, cells = [], 0
     batch = C.Batch()
     for n, amp, fe, fa, seed in specs:
@@ -571,36 +621,47 @@ def run_batch(args):
     t0 = time.perf_counter()
     policy, tuned_ms = batch.autotune(trial_steps=2)
     tune_s = time.perf_counter() - t0
-    batch.advance(args.warmup)
+    batch.advance(warmup)
     batch.sync()
-    t0 = time.perf_counter()
-    batch.advance(args.steps)
-    batch.sync()
-    el = time.perf_counter() - t0
+    ms = batch.advance_ms(steps)
     for b in boxes:
         b.sync()
-    value = cells * args.steps / el
-    # the first 32 boxes one at a time (each its own graph), for the batching efficiency
-    solo_cells, solo_t = 0, 0.0
-    for b, (n, *_r) in zip(boxes[:32], specs[:32]):
+    value = cells * steps / (ms * 1e-3)
+    solo_cells, solo_ms = 0, 0.0
+    for b, (n, *_r) in zip(boxes[:solo], specs[:solo]):
         batch.remove(b)
         b.advance(1)
         b.sync()
-        ts = time.perf_counter()
-        b.advance(5)
-        b.sync()
-        solo_t += time.perf_counter() - ts
+        solo_ms += b.advance_ms(5)
         solo_cells += n[0] * n[1] * n[2] * 5
-    res = {"workload": f"batch of {len(boxes)} uneven periodic boxes (16..96 per axis, seed 2), {args.precision}",
-           "cells_per_step": cells, "steps": args.steps, "value": value, "unit": "cell-updates/s",
-           "ms_per_step": 1e3 * el / args.steps, "autotune_policy": policy,
-           "autotune_ms_per_step_trial": tuned_ms, "autotune_s": tune_s, "launches_per_step": 7,
-           "first32_one_at_a_time_cell_updates_per_s": solo_cells / solo_t,
-           "device_bytes": sum(C.Box.bytes_for(s[0], prec) for s in specs)}
     batch.close()
     for b in boxes:
         b.close()
+    solo_rate = solo_cells / (solo_ms * 1e-3)
+    return {"boxes": len(specs), "cells_per_step": cells, "steps": steps, "value": value, "unit": "cell-updates/s",
+            "ms_per_step": ms / steps, "autotune_policy": policy, "autotune_s": tune_s, "launches_per_step": 7,
+            "first_boxes_one_at_a_time": {"boxes": solo, "value": solo_rate}, "batched_vs_one_at_a_time": value / solo_rate,
+            "device_bytes": sum(C.Box.bytes_for(sp[0], prec) for sp in specs)}
+
+
+def run_batch(args):
+    """--workload batch: 256 uneven boxes, --steps RK3 steps (the configuration's 50)."""
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    lib = C.load()
+    L.check(lib.cns_set_device(0))
+    prec = C.CNS_MIXED if args.precision == "mixed" else C.CNS_FP64
+    res = batch_run(C, prec, args.boxes, args.steps, args.warmup)
+    res["workload"] = f"batch of {args.boxes} uneven periodic boxes (16..96 per axis, seed 2), {args.precision}"
     return res
+
+
+def run_batch_short(C, args):
+    """The batch of 256 uneven boxes in both forms, a bounded number of steps (the default line)."""
+    steps = min(args.steps, 10)
+    return {"workload": "256 uneven periodic boxes (16..96 cells per axis, seed 2), one launch per kernel and stage, "
+                        f"graph-replayed, autotuned; {steps} timed steps",
+            "fp64": batch_run(C, C.CNS_FP64, 256, steps, 3), "mixed": batch_run(C, C.CNS_MIXED, 256, steps, 3)}
 
 
 def run_mixed256(args):
@@ -628,21 +689,17 @@ def run_mixed256(args):
             "rms_normwise_err": [float(x) for x in rms], "vars": ["rho", "rho u", "rho v", "rho w", "rho E"]}
 
 
-def run_serve(args):
+def serve_run(C, rate, requests, budget_gb, big, big_steps):
     """Poisson stream of independent solves (n 24..192, 10..200 steps, coefficients x U(0.8,1.2),
-    50/50 FP64/mixed), HBM budget, continuous batching; p50/p99 latency and throughput, beside
-    a single 512^3 FP64 box advanced alone."""
-    import cns_nospec_gb300 as C
-    from cns_nospec_gb300 import _lib as L
+    50/50 FP64/mixed), HBM budget, continuous batching: p50/p99 latency and throughput in real
+    time (arrivals honoured) and saturated (all waiting at t=0), the saturated run's efficiency
+    against the same solves at single-box rates, and a single big FP64 box advanced alone."""
     from cns_nospec_gb300 import initdata as I
     from cns_nospec_gb300 import serve as S
-    lib = C.load()
-    L.check(lib.cns_set_device(0))
-    reqs = S.request_stream(rate=args.rate, count=args.requests, seed=4)
-    srv = S.Server(budget_bytes=args.budget_gb * 1e9)
-    rep = srv.run(reqs, realtime=True)
-    sat = S.Server(budget_bytes=args.budget_gb * 1e9).run(
-        S.request_stream(rate=args.rate, count=args.requests, seed=5, start_all_at_zero=True), realtime=False)
+    srv = S.Server(budget_bytes=budget_gb * 1e9)
+    rep = srv.run(S.request_stream(rate=rate, count=requests, seed=4), realtime=True)
+    sat = S.Server(budget_bytes=budget_gb * 1e9).run(
+        S.request_stream(rate=rate, count=requests, seed=5, start_all_at_zero=True), realtime=False)
     # single-box throughput of each form, for the batching efficiency of the saturated run:
     # the time the same solves would take back to back, each at its form's 128^3 rate
     single = {}
@@ -650,30 +707,44 @@ def run_serve(args):
         b = C.Box(128, I.box_dx(128), I.CFL, I.ETA, I.ALAM, precision=prec)
         b.init_field((1.0, 1.0, 1.0), 1e-3, 1)
         b.autotune(trial_steps=2)
-        _, _, total = b.advance_timed(20)
-        b.sync()
-        single[prec] = 128 ** 3 * 20 / (total * 1e-3)
+        b.advance(3)
+        ms = b.advance_ms(20)
+        single[prec] = 128 ** 3 * 20 / (ms * 1e-3)
         b.close()
     # everything the device advanced (failed solves included) against the same cell-updates
     # at single-box rates: the loop's overhead and the batching gain for small boxes
     alone_s = sum(d.req.n[0] * d.req.n[1] * d.req.n[2] * d.steps_done / single[d.req.precision] for d in sat["done"])
     sat["single_box_rates"] = {"fp64": single[C.CNS_FP64], "mixed": single[C.CNS_MIXED]}
     sat["efficiency_vs_single_box"] = alone_s / sat["busy_s"] if sat["busy_s"] > 0 else None
-    big = {}
-    if args.big > 0:
-        n = args.big
-        b = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    sat["efficiency_vs_single_box_wall"] = alone_s / sat["wall_s"] if sat["wall_s"] > 0 else None
+    alone = {}
+    if big > 0:
+        b = C.Box(big, I.box_dx(big), I.CFL, I.ETA, I.ALAM)
         b.init_field((1.0, 1.0, 1.0), 1e-3, 1)
-        ms, _, total = b.advance_timed(args.big_steps)
-        b.sync()
-        big = {"n": n, "steps": args.big_steps, "cell_updates_per_s": n ** 3 * args.big_steps / (total * 1e-3),
-               "device_bytes": C.Box.bytes_for(n)}
+        b.advance(1)
+        ms = b.advance_ms(big_steps)
+        alone = {"n": big, "steps": big_steps, "cell_updates_per_s": big ** 3 * big_steps / (ms * 1e-3),
+                 "device_bytes": C.Box.bytes_for(big)}
         b.close()
     strip = lambda r: {k: v for k, v in r.items() if k != "done"}
-    return {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, n 24..192, steps 10..200, "
-                        f"50/50 FP64/mixed, budget {args.budget_gb} GB",
-            "realtime": strip(rep), "saturated": strip(sat), "single_box_alone": big,
+    return {"workload": f"{requests} requests, Poisson rate {rate}/s, n 24..192, steps 10..200, "
+                        f"50/50 FP64/mixed, budget {budget_gb} GB",
+            "realtime": strip(rep), "saturated": strip(sat), "single_box_alone": alone,
             "max_active": max((e["active"] for e in srv.log), default=0)}
+
+
+def run_serve(args):
+    """--workload serve: the request stream at --rate with --requests requests."""
+    import cns_nospec_gb300 as C
+    from cns_nospec_gb300 import _lib as L
+    lib = C.load()
+    L.check(lib.cns_set_device(0))
+    return serve_run(C, args.rate, args.requests, args.budget_gb, args.big, args.big_steps)
+
+
+def run_serve_short(C, args):
+    """A bounded serving stream for the default line: 32 requests at 3/s."""
+    return serve_run(C, 3.0, 32, 120.0, 512, 3)
 
 
 def main():
@@ -691,7 +762,7 @@ def main():
             res = run_reference(args, dist)
         else:
             res = run_ours(args, dist)
-            if dist.rank == 0 and res is not None and not args.no_cpu_baseline:
+            if dist.rank == 0 and dist.world == 1 and res is not None and not args.no_cpu_baseline:
                 res["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)
         if dist.rank == 0 and res is not None:
             print(json.dumps(res))

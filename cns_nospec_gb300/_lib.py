@@ -62,6 +62,7 @@ SIGNATURES = {
     "cns_fill_boundary": (C.c_int, [_D, _I, _I]),
     "cns_new_advance": (C.c_int, [C.POINTER(GlobalConst), _D, _D, _D, _D, _D, _D]),
     "cns_host_in_place": (C.c_int, [_VP, C.c_longlong, _I]),
+    "cns_set_pageable_in_place": (C.c_int, [C.c_int]),
     "cns_advance_host": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _D]),
     "cns_advance_f64": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, _D]),
     "cns_advance_mixed": (C.c_int, [_D, _I, _D, C.c_double, C.c_double, C.c_double, C.c_int, _D]),
@@ -75,6 +76,7 @@ SIGNATURES = {
     "cns_box_download_device": (C.c_int, [_VP, _VP]),
     "cns_box_advance": (C.c_int, [_VP, C.c_int]),
     "cns_box_advance_timed": (C.c_int, [_VP, C.c_int, _D, _I, _D]),
+    "cns_box_advance_ms": (C.c_int, [_VP, C.c_int, _D]),
     "cns_box_sync": (C.c_int, [_VP, _I]),
     "cns_box_last_dt": (C.c_int, [_VP, _D, _I]),
     "cns_box_launches_per_step": (C.c_int, [_VP]),
@@ -95,6 +97,7 @@ SIGNATURES = {
     "cns_batch_size": (C.c_int, [_VP]),
     "cns_batch_advance": (C.c_int, [_VP, C.c_int]),
     "cns_batch_sync": (C.c_int, [_VP]),
+    "cns_batch_advance_ms": (C.c_int, [_VP, C.c_int, _D]),
     "cns_box_get_tile": (C.c_int, [_VP, _I]),
     "cns_box_set_tile": (C.c_int, [_VP, _I]),
     "cns_box_autotune": (C.c_int, [_VP, C.c_int, _I, _I, _D]),

@@ -618,6 +618,37 @@ extern "C" int cns_box_advance(cns_box* b, int nsteps) {
     return CNS_OK;
 }
 
+// Device time of `launch` (graph replays on `st`) between two events on `st`; waits for it.
+template <class F>
+static int graph_ms(cudaStream_t st, F launch, double* ms) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    cudaError_t e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail_cuda(e, "cudaEventCreate", __LINE__);
+    }
+    int rc = CNS_OK;
+    e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) rc = launch();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float f = 0.f;
+    if (e == cudaSuccess && rc == CNS_OK) e = cudaEventElapsedTime(&f, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail_cuda(e, "graph timing", __LINE__);
+    if (ms) *ms = f;
+    return CNS_OK;
+}
+
+extern "C" int cns_box_advance_ms(cns_box* b, int nsteps, double* ms) {
+    if (!b) return fail(CNS_ERR_INVALID, "null box");
+    CK(cudaSetDevice(b->dev));
+    return graph_ms(b->stream, [&] { return cns_box_advance(b, nsteps); }, ms);
+}
+
 static int timed_run(cudaStream_t st, int nsteps, const BoxView* views, int nviews, const WorkLists& w,
                      double* kernel_ms, int* kernel_launches, double* total_ms) {
     std::vector<cudaEvent_t> ev;
@@ -857,6 +888,12 @@ extern "C" int cns_batch_advance(cns_batch* bt, int nsteps) {
     if (!bt->gexec) return CNS_OK;
     for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(bt->gexec, bt->stream));
     return CNS_OK;
+}
+
+extern "C" int cns_batch_advance_ms(cns_batch* bt, int nsteps, double* ms) {
+    if (!bt) return fail(CNS_ERR_INVALID, "null batch");
+    CK(cudaSetDevice(bt->dev));
+    return graph_ms(bt->stream, [&] { return cns_batch_advance(bt, nsteps); }, ms);
 }
 
 extern "C" int cns_batch_sync(cns_batch* bt) {
@@ -1185,6 +1222,11 @@ extern "C" int cns_advance_f64(double* U, const int n[3], const double dx[3], do
 extern "C" int cns_advance_mixed(double* U, const int n[3], const double dx[3], double cfl, double eta, double alam,
                                  int nsteps, double* dt_hist) {
     return cns_advance_host(U, n, dx, cfl, eta, alam, nsteps, CNS_MIXED, dt_hist);
+}
+
+extern "C" int cns_set_pageable_in_place(int enable) {
+    set_pageable_in_place(enable);
+    return CNS_OK;
 }
 
 extern "C" int cns_host_in_place(const void* U, long long bytes, int* in_place) {

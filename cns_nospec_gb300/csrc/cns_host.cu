@@ -17,10 +17,12 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <vector>
 
 #include "cns_fused.cuh"
+
 #include "cns_internal.h"
 
 namespace cns {
@@ -375,10 +377,37 @@ cudaError_t host_upload_deriv(const BoxView& v, double* h, bool ghosts, const Ti
     return cudaGetLastError();
 }
 
-// The device address of the host range [p, p + bytes) when all of it lies inside one
-// page-locked allocation that the device can address; otherwise null (the caller then stages
-// through a copy).  The range is checked against the allocation's extent as the driver records
-// it, so a kernel never touches host memory outside the caller's allocation.
+// The device address of the host range [p, p + bytes), or null (the caller then stages through
+// a copy).  Two kinds of host memory qualify:
+//  * page-locked memory (cudaHostAlloc, cudaHostRegister): when all of the range lies inside one
+//    such allocation that the device can address, checked against the allocation's extent as the
+//    driver records it, so a kernel never touches host memory outside the caller's allocation;
+//  * ordinary pageable memory (malloc, new, a numpy array), on a device that reads and writes it
+//    through the host's own page tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables: a
+//    GPU attached by NVLink-C2C, as on Grace-Blackwell), where the host address is the device
+//    address.  The range is then the caller's array as its dimensions give it, exactly as the
+//    reference's loops over the same array assume.  cns_set_pageable_in_place(0) turns this off.
+static std::atomic<int> g_pageable_in_place{1};
+
+static bool pageable_access(int dev) {
+    static std::atomic<int> cache[64];  // per device: 0 unknown, 1 no, 2 yes
+    if (dev < 0 || dev >= 64) return false;
+    int c = cache[dev].load();
+    if (c == 0) {
+        int pma = 0, hpt = 0;
+        if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            pma = hpt = 0;
+        }
+        c = (pma && hpt) ? 2 : 1;
+        cache[dev].store(c);
+    }
+    return c == 2;
+}
+
+void set_pageable_in_place(int enable) { g_pageable_in_place.store(enable ? 1 : 0); }
+
 typedef CUresult (*PointerGetAttributeFn)(void*, CUpointer_attribute, CUdeviceptr);
 
 static PointerGetAttributeFn pointer_attr_fn() {
@@ -398,6 +427,11 @@ void* mapped_host_range(const void* p, size_t bytes) {
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();  // not a pointer the runtime knows; clear the (non-sticky) error
         return nullptr;
+    }
+    if (a.type == cudaMemoryTypeUnregistered) {
+        int dev = -1;
+        if (!g_pageable_in_place.load() || cudaGetDevice(&dev) != cudaSuccess || !pageable_access(dev)) return nullptr;
+        return const_cast<void*>(p);
     }
     if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
     PointerGetAttributeFn get = pointer_attr_fn();

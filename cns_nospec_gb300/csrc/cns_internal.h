@@ -64,8 +64,9 @@ cudaError_t op_box_to_aos(const BoxView& b, double* aos, int ghosts, cudaStream_
 cudaError_t probe_fp64(double* tflops);
 
 // the reference-layout host array <-> a box over the CPU-GPU link, in place (cns_host.cu).
-// `h` is the device address of a page-locked host array (mapped_host_range).
+// `h` is the device address of a host array the device can address (mapped_host_range).
 void* mapped_host_range(const void* p, size_t bytes);
+void set_pageable_in_place(int enable);
 // ghosts: also write the host array's ghost cells (periodic images of its interior)
 cudaError_t host_upload(const BoxView& v, double* h, bool prim, bool ghosts, cudaStream_t st);
 cudaError_t host_download(const BoxView& v, double* h, cudaStream_t st);

@@ -3,8 +3,9 @@
 Requests (box size, step count, coefficients, precision tag) arrive over time.  The loop keeps
 every admitted box's state resident in HBM, admits waiting requests in arrival order whenever
 the device-memory budget (and an optional slot limit) allows, and advances ALL admitted boxes
-together one RK3 step per iteration through one cns_batch (one launch per kernel and stage for
-every box of a precision; each box keeps its own dt).  Boxes leave the batch as soon as they
+together through one cns_batch (one launch per kernel and stage for every box of a precision;
+each box keeps its own dt), as many RK3 steps per host round trip as the next event allows
+(a box reaching its step count, a health check, an expected arrival).  Boxes leave the batch as soon as they
 reach their step count, which frees their memory for the next arrivals.  Each box's result is
 bit-identical to the same solve run alone: every cell's arithmetic is independent of what
 else shares the launch.
@@ -113,7 +114,9 @@ class Server:
         batch = Batch_()
         used = 0
         peak_used = 0
-        iters = 0
+        iters = 0                       # host round trips (batch advances)
+        steps = 0                       # RK3 steps the batch ran
+        step_s = 0.0                    # measured device time of one batch step
         executed = 0
         busy = 0.0
         t0 = time.perf_counter()
@@ -141,19 +144,32 @@ class Server:
                     if pending and realtime:
                         time.sleep(max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 0.05)))
                     continue
+                # advance up to the next event without returning to the host in between: the
+                # first box to reach its step count, the next health check and, in real time,
+                # the next arrival (at the measured per-step time)
+                k = min(req.steps - steps_done for _, req, steps_done, *_r in active.values())
+                if self.health_every > 0:
+                    k = min(k, self.health_every - steps % self.health_every)
+                if realtime and pending and step_s > 0:
+                    wait = pending[0].arrival - (time.perf_counter() - t0)
+                    k = min(k, max(1, int(wait / step_s)))
+                k = max(1, k)
                 ts = time.perf_counter()
-                batch.advance(1)
+                batch.advance(k)
                 batch.sync()
-                busy += time.perf_counter() - ts
+                dt_busy = time.perf_counter() - ts
+                busy += dt_busy
+                step_s = dt_busy / k
                 iters += 1
-                executed += sum(r.n[0] * r.n[1] * r.n[2] for _, r, *_ in active.values())
+                steps += k
+                executed += k * sum(r.n[0] * r.n[1] * r.n[2] for _, r, *_ in active.values())
                 fin = time.perf_counter() - t0
-                check = self.health_every > 0 and iters % self.health_every == 0
+                check = self.health_every > 0 and steps % self.health_every == 0
                 for rid in list(active):
-                    box, req, k, need, adm = active[rid]
-                    k += 1
+                    box, req, n_done, need, adm = active[rid]
+                    n_done += k
                     # evict a diverged solve early instead of running it to its last step
-                    if k >= req.steps or (check and box.health()):
+                    if n_done >= req.steps or (check and box.health()):
                         batch.remove(box)
                         # a solve whose state went non-physical fails alone; the others go on
                         health = box.health()
@@ -161,9 +177,9 @@ class Server:
                         box.close()
                         used -= need
                         del active[rid]
-                        done.append(Done(req, adm, fin, res, health, k))
+                        done.append(Done(req, adm, fin, res, health, n_done))
                     else:
-                        active[rid] = (box, req, k, need, adm)
+                        active[rid] = (box, req, n_done, need, adm)
         finally:
             for box, *_ in active.values():
                 box.close()
@@ -186,7 +202,8 @@ class Server:
             "executed_per_busy_s": executed / max(busy, 1e-9),
             "busy_s": busy,
             "wall_s": wall,
-            "iterations": iters,
+            "host_round_trips": iters,
+            "batch_steps": steps,
             "peak_bytes": peak_used,
             "done": done,
         }

@@ -168,6 +168,13 @@ class Box:
     def advance(self, nsteps):
         L.check(self.lib.cns_box_advance(self.h, int(nsteps)))
 
+    def advance_ms(self, nsteps) -> float:
+        """nsteps graph-replayed RK3 steps; waits for them and returns their device time (ms,
+        CUDA events on the box's stream)."""
+        ms = C.c_double()
+        L.check(self.lib.cns_box_advance_ms(self.h, int(nsteps), C.byref(ms)))
+        return ms.value
+
     def advance_timed(self, nsteps):
         ms = (C.c_double * L.KERN_COUNT)()
         launches = (C.c_int * L.KERN_COUNT)()
@@ -251,6 +258,12 @@ class Batch:
 
     def advance(self, nsteps=1):
         L.check(self.lib.cns_batch_advance(self.h, int(nsteps)))
+
+    def advance_ms(self, nsteps) -> float:
+        """nsteps graph-replayed steps of every member; waits and returns their device time (ms)."""
+        ms = C.c_double()
+        L.check(self.lib.cns_batch_advance_ms(self.h, int(nsteps), C.byref(ms)))
+        return ms.value
 
     def sync(self):
         L.check(self.lib.cns_batch_sync(self.h))

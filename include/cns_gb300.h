@@ -142,13 +142,22 @@ int cns_advance_f64(double *U, const int n[3], const double dx[3], double cfl, d
 int cns_advance_mixed(double *U, const int n[3], const double dx[3], double cfl, double eta, double alam, int nsteps,
                       double *dt_hist);
 
-/* Host arrays: when all of [U, U + bytes) lies in one page-locked allocation the device can
- * address (cudaHostAlloc, cudaHostRegister, a pinned torch tensor), cns_new_advance,
- * cns_advance_host, cns_box_upload and cns_box_download read and write it in place from the
- * GPU over the CPU-GPU link (interior only on the way in; no staging copy); any other host
- * memory is staged through a device buffer.  Results are bit-identical either way.
+/* Host arrays: cns_new_advance, cns_advance_host, cns_box_upload and cns_box_download read and
+ * write the caller's array in place from the GPU over the CPU-GPU link (interior only on the
+ * way in; no staging copy) when
+ *  - all of [U, U + bytes) lies in one page-locked allocation the device can address
+ *    (cudaHostAlloc, cudaHostRegister, a pinned torch tensor), or
+ *  - U is ordinary pageable memory (malloc, as the reference's allocate_4D uses) and the device
+ *    reads host memory through the host's page tables (NVLink-C2C, as on Grace-Blackwell); the
+ *    array must then hold the [n0+8][n1+8][n2+8][5] doubles its dimensions give, as it must for
+ *    the reference's own loops.
+ * Any other host memory is staged through a device buffer.  Results are bit-identical either way.
  * *in_place = 1 when `U` takes the in-place path.  No counterpart in the reference. */
 int cns_host_in_place(const void *U, long long bytes, int *in_place);
+/* enable = 0: pageable host arrays take the staged path even where the device could use them in
+ * place (page-locked arrays are unaffected); 1 (the default): in place where the device can.
+ * Process-wide.  No counterpart in the reference. */
+int cns_set_pageable_in_place(int enable);
 
 /* ---- device-resident boxes ------------------------------------------------------------- */
 typedef struct cns_box cns_box;
@@ -175,6 +184,9 @@ int cns_box_upload_device(cns_box *box, const double *U_dev);
 int cns_box_download_device(cns_box *box, double *U_dev);
 /* nsteps RK3 steps, asynchronous on the box's stream (replays a captured one-step graph). */
 int cns_box_advance(cns_box *box, int nsteps);
+/* cns_box_advance bracketed by two CUDA events on the box's stream: waits for the steps and
+ * returns their device time in *ms (no counterpart in the reference; for benchmarks). */
+int cns_box_advance_ms(cns_box *box, int nsteps, double *ms);
 /* Same, without graphs, with a CUDA event around every kernel launch; fills
  * kernel_ms[CNS_KERN_COUNT] (summed device ms per kernel kind), kernel_launches[...] and
  * *total_ms (first to last event).  Blocks until done. */
@@ -223,6 +235,9 @@ int cns_batch_size(const cns_batch *batch);
  * one step (rebuilt when membership changes).  Asynchronous. */
 int cns_batch_advance(cns_batch *batch, int nsteps);
 int cns_batch_sync(cns_batch *batch);
+/* cns_batch_advance bracketed by two CUDA events on the batch's stream: waits for the steps
+ * and returns their device time in *ms (no counterpart in the reference; for benchmarks). */
+int cns_batch_advance_ms(cns_batch *batch, int nsteps, double *ms);
 
 /* ---- tile shapes and the autotuner -------------------------------------------------------
  * Work is cut into tiles of 256 cells (one per thread, k fastest across a warp); a box's tile

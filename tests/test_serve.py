@@ -151,3 +151,27 @@ def test_diverging_box_does_not_disturb_its_batch(gpu, cns):
         assert b.health() == 0
         assert np.array_equal(b.download(), S.run_alone(r))
     batch.close()
+
+
+@pytest.mark.gpu
+def test_served_results_match_the_oracle(gpu, cns, oracle):
+    """Every result of a small mixed stream (FP64 and mixed requests, uneven n <= 40) against the
+    reference algorithm (the oracle, cpu/advance.cpp:13-154) run on the same initial state: the
+    FP64 requests within the FP64 parity bar, the mixed ones within the mixed form's bar."""
+    from conftest import FP64_TOL, MIXED_TOL
+    from cns_nospec_gb300 import initdata as I
+    reqs = S.request_stream(rate=50.0, count=8, seed=21, nmin=16, nmax=40, smin=4, smax=12)
+    assert {r.precision for r in reqs} == {cns.CNS_FP64, cns.CNS_MIXED}
+    budget = 2.2 * max(cns.Box.bytes_for(r.n, r.precision) for r in reqs)
+    rep = S.Server(budget_bytes=budget, keep_results=True).run(reqs, realtime=False)
+    assert rep["requests"] == len(reqs) and rep["failed"] == 0
+    assert rep["host_round_trips"] < rep["batch_steps"]   # several steps per round trip
+    for d in rep["done"]:
+        r = d.req
+        b = cns.Box(r.n, I.box_dx(r.n), I.CFL, r.eta, r.alam)
+        b.init_field(r.amp, r.perturb, r.seed)     # the same device-generated initial state
+        U0 = b.download()
+        b.close()
+        ref, _ = oracle.advance(U0, r.steps, I.box_dx(r.n), I.CFL, r.eta, r.alam)
+        err = I.normwise_error(d.result, ref)[0]
+        assert err.max() <= (FP64_TOL if r.precision == cns.CNS_FP64 else MIXED_TOL), (r, err)
