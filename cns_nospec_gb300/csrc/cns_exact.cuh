@@ -89,7 +89,8 @@ __host__ __device__ __forceinline__ void xtap(long long& L, long long& H, double
     H += (long long)ws * (int)(t >> 31);
 }
 
-// (H * 2^31 + L) * 2^e2 rounded to nearest even; false when outside the normal range.
+// (H * 2^31 + L) * 2^e2 rounded to nearest even; false when outside the normal range.  *out is
+// written in every case (with an unspecified value when false), so that callers need no branch.
 __host__ __device__ __forceinline__ bool xround(long long H, long long L, int e2, double* out) {
     H += L >> 31;
     const unsigned l = (unsigned)L & 0x7FFFFFFFu;  // S = H 2^31 + l, 0 <= l < 2^31
@@ -97,10 +98,7 @@ __host__ __device__ __forceinline__ bool xround(long long H, long long L, int e2
     // |S| = mh 2^31 + ml with ml < 2^31
     const unsigned long long mh = !neg ? (unsigned long long)H : (l ? (unsigned long long)~H : (unsigned long long)-H);
     const unsigned ml = !neg ? l : (l ? 0x80000000u - l : 0u);
-    if (mh == 0 && ml == 0) {
-        *out = 0.0;
-        return true;
-    }
+    const bool zero = (mh | ml) == 0;
     unsigned long long top;  // |S| with its leading bit at 63
     bool sticky = false;
     int p;  // position of the leading bit of |S|
@@ -115,22 +113,25 @@ __host__ __device__ __forceinline__ bool xround(long long H, long long L, int e2
             top = (mh << z) | ((unsigned long long)ml << (z - 31));
         }
     } else {
-        const int z = xclz64((unsigned long long)ml);  // >= 33
+        const unsigned long long m1 = zero ? 1ull : (unsigned long long)ml;  // no clz of 0
+        const int z = xclz64(m1);  // >= 33
         p = 63 - z;
-        top = (unsigned long long)ml << z;
+        top = m1 << z;
     }
     unsigned long long q = top >> 11;
     const unsigned rem = (unsigned)top & 0x7FFu;
     q += (rem > 0x400u || (rem == 0x400u && (sticky || (q & 1ull)))) ? 1ull : 0ull;
     const int be = p + e2 + 1023;
-    if (be < 1 || be > 2045) return false;
-    *out = xbits(((unsigned long long)(be - 1) << 52) + q | (neg ? 0x8000000000000000ull : 0ull));
-    return true;
+    const unsigned long long bits =
+        ((unsigned long long)(be - 1) << 52) + q | (neg ? 0x8000000000000000ull : 0ull);
+    *out = zero ? 0.0 : xbits(bits);
+    return zero || (be >= 1 && be <= 2045);
 }
 
-// sum_{m=1..4} w_m (ld(m) + SGN ld(-m)), exactly, rounded once; false (and *out untouched)
-// for taps that are not finite or a sum outside the normal range.  ld(m) returns the tap at
-// offset m; SGN = -1 for first derivatives, +1 for the off-centre part of second derivatives.
+// sum_{m=1..4} w_m (ld(m) + SGN ld(-m)), exactly, rounded once; false for taps that are not
+// finite or a sum outside the normal range (*out is then written with an unspecified value).
+// ld(m) returns the tap at offset m; SGN = -1 for first derivatives, +1 for the off-centre part
+// of second derivatives.
 template <int W1, int W2, int W3, int W4, int SGN, class Ld>
 __host__ __device__ __forceinline__ bool xsum8(const Ld& ld, double* out) {
     const double a1 = ld(1), a2 = ld(2), a3 = ld(3), a4 = ld(4);
@@ -145,7 +146,6 @@ __host__ __device__ __forceinline__ bool xsum8(const Ld& ld, double* out) {
     f = xmax(f, xfield(a4));
     f = xmax(f, xfield(b4));
     const int emax = f >> 20;
-    if (emax == 0x7FF) return false;
     long long L = 0, H = 0;
     xtap(L, H, a1, emax, W1);
     xtap(L, H, b1, emax, SGN * W1);
@@ -155,7 +155,8 @@ __host__ __device__ __forceinline__ bool xsum8(const Ld& ld, double* out) {
     xtap(L, H, b3, emax, SGN * W3);
     xtap(L, H, a4, emax, W4);
     xtap(L, H, b4, emax, SGN * W4);
-    return xround(H, L, emax - 1075 - kXGuard, out);
+    const bool ok = xround(H, L, emax - 1075 - kXGuard, out);
+    return ok && emax != 0x7FF;
 }
 
 // The exact stencils with their FP64 fallbacks.  a[0..3] are the chain's coefficients
@@ -177,6 +178,22 @@ __host__ __device__ __forceinline__ double xd2acc(double acc, const Ld& ld, cons
     acc = fma(b[1], ld(2) + ld(-2), acc);
     acc = fma(b[2], ld(3) + ld(-3), acc);
     return fma(b[3], ld(4) + ld(-4), acc);
+}
+// The same without the fallback branch: the exact result whatever the taps, and *fail set where
+// xd1acc / xd2acc would have taken the FP64 chain.  A caller evaluates a whole cell this way,
+// with no branch between its stencils, and evaluates the cell again with xd1acc / xd2acc when
+// *fail is set; every stencil then gives the bits xd1acc / xd2acc give.
+template <class Ld>
+__host__ __device__ __forceinline__ double xd1acc_nb(double acc, const Ld& ld, const double* a, bool* fail) {
+    double x;
+    *fail |= !xsum8<672, -168, 32, -3, -1>(ld, &x);
+    return fma(a[4], x, acc);
+}
+template <class Ld>
+__host__ __device__ __forceinline__ double xd2acc_nb(double acc, const Ld& ld, const double* b, bool* fail) {
+    double x;
+    *fail |= !xsum8<8064, -1008, 128, -9, 1>(ld, &x);
+    return fma(b[4], x, acc);
 }
 
 // Tap loaders: a strided array (global memory through a chosen load, or shared memory) and a

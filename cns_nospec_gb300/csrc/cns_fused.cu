@@ -72,54 +72,19 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
             const R* Pr = (const R*)b.P[pr];
             R* Pw = (R*)b.P[pr ^ 1];
             const R* S = (const R*)b.S;
-            const long long c = cell_off(b, i, j, k), fs = b.fs, si = b.si, sj = b.sj;
-            const CoefT<R>& cf = coefs<R>(b);
-            const R* pu = Pr + PU * fs + c;
-            const R* pv = Pr + PV * fs + c;
-            const R* pw = Pr + PW * fs + c;
-            const R* pt = Pr + PT * fs + c;
-            const R u0 = ld(pu), v0 = ld(pv), w0 = ld(pw), t0 = ld(pt);
-            // diffterm momentum components (cpu/diffterm.cpp:155-269)
-            R dmx = cf.vc[0] * u0;
-            dmx = d2acc<xon(kExactLap, 0)>(dmx, pu, si, cf.vl[0][0]);
-            dmx = d2acc<xon(kExactLap, 1)>(dmx, pu, sj, cf.vl[0][1]);
-            dmx = d2acc<xon(kExactLap, 2)>(dmx, pu, 1, cf.vl[0][2]);
-            dmx = d1acc<xon(kExactMixed, 0)>(dmx, S + SX * fs + c, si, cf.mx[0]);
-            R dmy = cf.vc[1] * v0;
-            dmy = d2acc<xon(kExactLap, 0)>(dmy, pv, si, cf.vl[1][0]);
-            dmy = d2acc<xon(kExactLap, 1)>(dmy, pv, sj, cf.vl[1][1]);
-            dmy = d2acc<xon(kExactLap, 2)>(dmy, pv, 1, cf.vl[1][2]);
-            dmy = d1acc<xon(kExactMixed, 1)>(dmy, S + SY * fs + c, sj, cf.mx[1]);
-            R dmz = cf.vc[2] * w0;
-            dmz = d2acc<xon(kExactLap, 0)>(dmz, pw, si, cf.vl[2][0]);
-            dmz = d2acc<xon(kExactLap, 1)>(dmz, pw, sj, cf.vl[2][1]);
-            dmz = d2acc<xon(kExactLap, 2)>(dmz, pw, 1, cf.vl[2][2]);
-            dmz = d1acc<xon(kExactMixed, 2)>(dmz, S + SZ * fs + c, 1, cf.mx[2]);
-            // diffterm energy component (cpu/diffterm.cpp:272-311)
-            R de = fma(cf.tc, t0, ld(S + SPHI * fs + c));
-            de = d2acc<xon(kExactLap, 0)>(de, pt, si, cf.tl[0]);
-            de = d2acc<xon(kExactLap, 1)>(de, pt, sj, cf.tl[1]);
-            de = d2acc<xon(kExactLap, 2)>(de, pt, 1, cf.tl[2]);
-            de = fma(dmx, u0, de);
-            de = fma(dmy, v0, de);
-            de = fma(dmz, w0, de);
-            // hypterm (cpu/hypterm.cpp:29-208), added to D
+            const long long c = cell_off(b, i, j, k), fs = b.fs;
+            const R u0 = ld(Pr + PU * fs + c), v0 = ld(Pr + PV * fs + c), w0 = ld(Pr + PW * fs + c),
+                    t0 = ld(Pr + PT * fs + c);
+            // diffterm + hypterm (cpu/diffterm.cpp:155-311, cpu/hypterm.cpp:29-208); the plain form
+            // with no branch between its exact sums, again with their fallbacks where one needs it
             R f[5];
-            f[0] = d1<xon(kExactFlux, 0)>(Pr + PMX * fs + c, si, cf.ha[0]);
-            f[0] = d1acc<xon(kExactFlux, 1)>(f[0], Pr + PMY * fs + c, sj, cf.ha[1]);
-            f[0] = d1acc<xon(kExactFlux, 2)>(f[0], Pr + PMZ * fs + c, 1, cf.ha[2]);
-            f[1] = d1acc<xon(kExactFlux, 0)>(dmx, Pr + PFUU * fs + c, si, cf.ha[0]);
-            f[1] = d1acc<xon(kExactFlux, 1)>(f[1], Pr + PFUV * fs + c, sj, cf.ha[1]);
-            f[1] = d1acc<xon(kExactFlux, 2)>(f[1], Pr + PFUW * fs + c, 1, cf.ha[2]);
-            f[2] = d1acc<xon(kExactFlux, 0)>(dmy, Pr + PFUV * fs + c, si, cf.ha[0]);
-            f[2] = d1acc<xon(kExactFlux, 1)>(f[2], Pr + PFVV * fs + c, sj, cf.ha[1]);
-            f[2] = d1acc<xon(kExactFlux, 2)>(f[2], Pr + PFVW * fs + c, 1, cf.ha[2]);
-            f[3] = d1acc<xon(kExactFlux, 0)>(dmz, Pr + PFUW * fs + c, si, cf.ha[0]);
-            f[3] = d1acc<xon(kExactFlux, 1)>(f[3], Pr + PFVW * fs + c, sj, cf.ha[1]);
-            f[3] = d1acc<xon(kExactFlux, 2)>(f[3], Pr + PFWW * fs + c, 1, cf.ha[2]);
-            f[4] = d1acc<xon(kExactFlux, 0)>(de, Pr + PHU * fs + c, si, cf.ha[0]);
-            f[4] = d1acc<xon(kExactFlux, 1)>(f[4], Pr + PHV * fs + c, sj, cf.ha[1]);
-            f[4] = d1acc<xon(kExactFlux, 2)>(f[4], Pr + PHW * fs + c, 1, cf.ha[2]);
+            if constexpr (sizeof(R) == 8) {
+                bool xf = false;
+                assemble_terms<R, true>(b, Pr, S, c, u0, v0, w0, t0, f, &xf);
+                if (xf) assemble_terms_fallback<R>(b, Pr, S, c, u0, v0, w0, t0, f);
+            } else {
+                assemble_terms<R, false>(b, Pr, S, c, u0, v0, w0, t0, f, nullptr);
+            }
             if (sizeof(R) == 4) {
                 // mixed form: the P set holds ((E + p) - H_ref) u_d, so add -H_ref div(u);
                 // div(u) = (S_x + S_y + S_z) / 2 with the same first-difference operator

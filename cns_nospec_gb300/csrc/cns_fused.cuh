@@ -43,9 +43,14 @@ template <>
 __device__ __forceinline__ const CoefT<float>& coefs<float>(const BoxView& b) { return b.c32; }
 
 // acc + sum_m a_m (p[m s] - p[-m s]); in the plain form (R = double) the exact sum (cns_exact.cuh)
-template <bool X, class R>
-__device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, const R* a) {
-    if constexpr (sizeof(R) == 8 && X) return xd1acc(acc, XTaps<0>{p, s}, a);
+// where X.  NB (no branch): the exact sum without its FP64 fallback, *xf set where the fallback
+// is needed (the caller then evaluates the cell again with NB = false; cns_exact.cuh).
+template <bool X, class R, bool NB = false>
+__device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, const R* a, bool* xf = nullptr) {
+    if constexpr (sizeof(R) == 8 && X) {
+        if constexpr (NB) return xd1acc_nb(acc, XTaps<0>{p, s}, a, xf);
+        else return xd1acc(acc, XTaps<0>{p, s}, a);
+    }
     acc = fma(a[0], __ldg(p + s) - __ldg(p - s), acc);
     acc = fma(a[1], __ldg(p + 2 * s) - __ldg(p - 2 * s), acc);
     acc = fma(a[2], __ldg(p + 3 * s) - __ldg(p - 3 * s), acc);
@@ -60,9 +65,12 @@ __device__ __forceinline__ R ld_tap(const R* p) {
     if (NC) return __ldg(p);
     return __ldcg(p);
 }
-template <bool X, class R, bool NC = true>
-__device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a) {
-    if constexpr (sizeof(R) == 8 && X) return xd1acc(0.0, XTaps<NC ? 0 : 1>{p, s}, a);
+template <bool X, class R, bool NC = true, bool NB = false>
+__device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a, bool* xf = nullptr) {
+    if constexpr (sizeof(R) == 8 && X) {
+        if constexpr (NB) return xd1acc_nb(0.0, XTaps<NC ? 0 : 1>{p, s}, a, xf);
+        else return xd1acc(0.0, XTaps<NC ? 0 : 1>{p, s}, a);
+    }
     R acc = a[0] * (ld_tap<NC>(p + s) - ld_tap<NC>(p - s));
     acc = fma(a[1], ld_tap<NC>(p + 2 * s) - ld_tap<NC>(p - 2 * s), acc);
     acc = fma(a[2], ld_tap<NC>(p + 3 * s) - ld_tap<NC>(p - 3 * s), acc);
@@ -70,9 +78,12 @@ __device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a
     return acc;
 }
 // acc + sum_m b_m (p[m s] + p[-m s])
-template <bool X, class R>
-__device__ __forceinline__ R d2acc(R acc, const R* __restrict__ p, long long s, const R* b) {
-    if constexpr (sizeof(R) == 8 && X) return xd2acc(acc, XTaps<0>{p, s}, b);
+template <bool X, class R, bool NB = false>
+__device__ __forceinline__ R d2acc(R acc, const R* __restrict__ p, long long s, const R* b, bool* xf = nullptr) {
+    if constexpr (sizeof(R) == 8 && X) {
+        if constexpr (NB) return xd2acc_nb(acc, XTaps<0>{p, s}, b, xf);
+        else return xd2acc(acc, XTaps<0>{p, s}, b);
+    }
     acc = fma(b[0], __ldg(p + s) + __ldg(p - s), acc);
     acc = fma(b[1], __ldg(p + 2 * s) + __ldg(p - 2 * s), acc);
     acc = fma(b[2], __ldg(p + 3 * s) + __ldg(p - 3 * s), acc);
@@ -159,8 +170,36 @@ __device__ __forceinline__ void dissipation(R ux, R uy, R uz, R vx, R vy, R vz, 
     *phi = f;
 }
 
+// The nine first derivatives of (u, v, w) at one cell (cpu/diffterm.cpp:73-151); NB as in d1.
+template <class R, bool NC, bool NB>
+__device__ __forceinline__ void deriv9(const R* pu, const R* pv, const R* pw, long long si, long long sj,
+                                       const CoefT<R>& cf, R (&d)[9], bool* xf) {
+    constexpr bool X0 = xon(kExactDeriv, 0), X1 = xon(kExactDeriv, 1), X2 = xon(kExactDeriv, 2);
+    d[0] = d1<X0, R, NC, NB>(pu, si, cf.da[0], xf);
+    d[1] = d1<X1, R, NC, NB>(pu, sj, cf.da[1], xf);
+    d[2] = d1<X2, R, NC, NB>(pu, 1, cf.da[2], xf);
+    d[3] = d1<X0, R, NC, NB>(pv, si, cf.da[0], xf);
+    d[4] = d1<X1, R, NC, NB>(pv, sj, cf.da[1], xf);
+    d[5] = d1<X2, R, NC, NB>(pv, 1, cf.da[2], xf);
+    d[6] = d1<X0, R, NC, NB>(pw, si, cf.da[0], xf);
+    d[7] = d1<X1, R, NC, NB>(pw, sj, cf.da[1], xf);
+    d[8] = d1<X2, R, NC, NB>(pw, 1, cf.da[2], xf);
+}
+
+// deriv9 with the exact sums' fallbacks, out of line (as assemble_terms_fallback).
+template <class R, bool NC>
+__device__ __noinline__ void deriv9_fallback(const R* pu, const R* pv, const R* pw, long long si, long long sj,
+                                             const CoefT<R>& cf, R* d) {
+    R g[9];
+    deriv9<R, NC, false>(pu, pv, pw, si, sj, cf, g, nullptr);
+#pragma unroll
+    for (int l = 0; l < 9; l++) d[l] = g[l];
+}
+
 // k_deriv's work at cell (i, j, k) of stage `stage`: the nine first derivatives of (u, v, w)
-// (cpu/diffterm.cpp:73-151) into the S sums and the viscous dissipation (cpu/diffterm.cpp:294-304).
+// into the S sums and the viscous dissipation (cpu/diffterm.cpp:294-304).  The plain form
+// evaluates the derivatives with no branch between its exact sums and again with their
+// fallbacks in the rare cell that needs one (the same bits either way).
 // NC = false reads the P set from L2 (ld_tap), for a launch whose other blocks write it.
 template <class R, bool NC = true>
 __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k, int stage) {
@@ -172,18 +211,86 @@ __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k
     const R* pu = P + PU * fs + c;
     const R* pv = P + PV * fs + c;
     const R* pw = P + PW * fs + c;
-    constexpr bool X0 = xon(kExactDeriv, 0), X1 = xon(kExactDeriv, 1), X2 = xon(kExactDeriv, 2);
-    const R ux = d1<X0, R, NC>(pu, si, cf.da[0]), uy = d1<X1, R, NC>(pu, sj, cf.da[1]), uz = d1<X2, R, NC>(pu, 1, cf.da[2]);
-    const R vx = d1<X0, R, NC>(pv, si, cf.da[0]), vy = d1<X1, R, NC>(pv, sj, cf.da[1]), vz = d1<X2, R, NC>(pv, 1, cf.da[2]);
-    const R wx = d1<X0, R, NC>(pw, si, cf.da[0]), wy = d1<X1, R, NC>(pw, sj, cf.da[1]), wz = d1<X2, R, NC>(pw, 1, cf.da[2]);
+    R d[9];
+    if constexpr (sizeof(R) == 8) {
+        bool xf = false;
+        deriv9<R, NC, true>(pu, pv, pw, si, sj, cf, d, &xf);
+        if (xf) deriv9_fallback<R, NC>(pu, pv, pw, si, sj, cf, d);
+    } else {
+        deriv9<R, NC, false>(pu, pv, pw, si, sj, cf, d, nullptr);
+    }
     R sx, sy, sz, phi;
-    dissipation(ux, uy, uz, vx, vy, vz, wx, wy, wz, &sx, &sy, &sz, &phi);
+    dissipation(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], &sx, &sy, &sz, &phi);
     store_img(S + SX * fs, b, c, i, j, k, sx, 1);
     store_img(S + SY * fs, b, c, i, j, k, sy, 2);
     store_img(S + SZ * fs, b, c, i, j, k, sz, 4);
     S[SPHI * fs + c] = cf.eta * phi;
 }
 
+// diffterm + hypterm of one cell (cpu/diffterm.cpp:155-311, cpu/hypterm.cpp:29-208) from the P set
+// Pr and the S set at element c: f[l] = D[l] + F[l].  NB as in d1.
+template <class R, bool NB>
+__device__ __forceinline__ void assemble_terms(const BoxView& b, const R* __restrict__ Pr, const R* __restrict__ S,
+                                               long long c, R u0, R v0, R w0, R t0, R (&f)[5], bool* xf) {
+    const long long fs = b.fs, si = b.si, sj = b.sj;
+    const CoefT<R>& cf = coefs<R>(b);
+    const R* pu = Pr + PU * fs + c;
+    const R* pv = Pr + PV * fs + c;
+    const R* pw = Pr + PW * fs + c;
+    const R* pt = Pr + PT * fs + c;
+    // diffterm momentum components (cpu/diffterm.cpp:155-269)
+    R dmx = cf.vc[0] * u0;
+    dmx = d2acc<xon(kExactLap, 0), R, NB>(dmx, pu, si, cf.vl[0][0], xf);
+    dmx = d2acc<xon(kExactLap, 1), R, NB>(dmx, pu, sj, cf.vl[0][1], xf);
+    dmx = d2acc<xon(kExactLap, 2), R, NB>(dmx, pu, 1, cf.vl[0][2], xf);
+    dmx = d1acc<xon(kExactMixed, 0), R, NB>(dmx, S + SX * fs + c, si, cf.mx[0], xf);
+    R dmy = cf.vc[1] * v0;
+    dmy = d2acc<xon(kExactLap, 0), R, NB>(dmy, pv, si, cf.vl[1][0], xf);
+    dmy = d2acc<xon(kExactLap, 1), R, NB>(dmy, pv, sj, cf.vl[1][1], xf);
+    dmy = d2acc<xon(kExactLap, 2), R, NB>(dmy, pv, 1, cf.vl[1][2], xf);
+    dmy = d1acc<xon(kExactMixed, 1), R, NB>(dmy, S + SY * fs + c, sj, cf.mx[1], xf);
+    R dmz = cf.vc[2] * w0;
+    dmz = d2acc<xon(kExactLap, 0), R, NB>(dmz, pw, si, cf.vl[2][0], xf);
+    dmz = d2acc<xon(kExactLap, 1), R, NB>(dmz, pw, sj, cf.vl[2][1], xf);
+    dmz = d2acc<xon(kExactLap, 2), R, NB>(dmz, pw, 1, cf.vl[2][2], xf);
+    dmz = d1acc<xon(kExactMixed, 2), R, NB>(dmz, S + SZ * fs + c, 1, cf.mx[2], xf);
+    // diffterm energy component (cpu/diffterm.cpp:272-311)
+    R de = fma(cf.tc, t0, __ldg(S + SPHI * fs + c));
+    de = d2acc<xon(kExactLap, 0), R, NB>(de, pt, si, cf.tl[0], xf);
+    de = d2acc<xon(kExactLap, 1), R, NB>(de, pt, sj, cf.tl[1], xf);
+    de = d2acc<xon(kExactLap, 2), R, NB>(de, pt, 1, cf.tl[2], xf);
+    de = fma(dmx, u0, de);
+    de = fma(dmy, v0, de);
+    de = fma(dmz, w0, de);
+    // hypterm (cpu/hypterm.cpp:29-208), added to D
+    f[0] = d1<xon(kExactFlux, 0), R, true, NB>(Pr + PMX * fs + c, si, cf.ha[0], xf);
+    f[0] = d1acc<xon(kExactFlux, 1), R, NB>(f[0], Pr + PMY * fs + c, sj, cf.ha[1], xf);
+    f[0] = d1acc<xon(kExactFlux, 2), R, NB>(f[0], Pr + PMZ * fs + c, 1, cf.ha[2], xf);
+    f[1] = d1acc<xon(kExactFlux, 0), R, NB>(dmx, Pr + PFUU * fs + c, si, cf.ha[0], xf);
+    f[1] = d1acc<xon(kExactFlux, 1), R, NB>(f[1], Pr + PFUV * fs + c, sj, cf.ha[1], xf);
+    f[1] = d1acc<xon(kExactFlux, 2), R, NB>(f[1], Pr + PFUW * fs + c, 1, cf.ha[2], xf);
+    f[2] = d1acc<xon(kExactFlux, 0), R, NB>(dmy, Pr + PFUV * fs + c, si, cf.ha[0], xf);
+    f[2] = d1acc<xon(kExactFlux, 1), R, NB>(f[2], Pr + PFVV * fs + c, sj, cf.ha[1], xf);
+    f[2] = d1acc<xon(kExactFlux, 2), R, NB>(f[2], Pr + PFVW * fs + c, 1, cf.ha[2], xf);
+    f[3] = d1acc<xon(kExactFlux, 0), R, NB>(dmz, Pr + PFUW * fs + c, si, cf.ha[0], xf);
+    f[3] = d1acc<xon(kExactFlux, 1), R, NB>(f[3], Pr + PFVW * fs + c, sj, cf.ha[1], xf);
+    f[3] = d1acc<xon(kExactFlux, 2), R, NB>(f[3], Pr + PFWW * fs + c, 1, cf.ha[2], xf);
+    f[4] = d1acc<xon(kExactFlux, 0), R, NB>(de, Pr + PHU * fs + c, si, cf.ha[0], xf);
+    f[4] = d1acc<xon(kExactFlux, 1), R, NB>(f[4], Pr + PHV * fs + c, sj, cf.ha[1], xf);
+    f[4] = d1acc<xon(kExactFlux, 2), R, NB>(f[4], Pr + PHW * fs + c, 1, cf.ha[2], xf);
+}
+
+// assemble_terms with the exact sums' fallbacks, out of line: the rare cell that needs one takes
+// a call, and the fast path's registers are allocated without this copy of the code beside it.
+template <class R>
+__device__ __noinline__ void assemble_terms_fallback(const BoxView& b, const R* __restrict__ Pr,
+                                                     const R* __restrict__ S, long long c, R u0, R v0, R w0, R t0,
+                                                     R* f) {
+    R g[5];
+    assemble_terms<R, false>(b, Pr, S, c, u0, v0, w0, t0, g, nullptr);
+#pragma unroll
+    for (int l = 0; l < 5; l++) f[l] = g[l];
+}
 // Health bits from raw IEEE fields (integer ops only; no FP64 pipe work).
 __device__ __forceinline__ int health_bits(double rho, double eint) {
     unsigned long long rb = dbits(rho), eb = dbits(eint);
