@@ -211,8 +211,9 @@ def cpu_baseline(n: int, seconds: float):
     from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
     O.build(ref=os.path.isdir(O.REF_SRC))
-    nproc = host_processes(n)
-    value, steps, wall = oracle_processes(n, 1000, 1, seconds, nproc)
+    threads = host_split("port")
+    nproc = host_processes(n, threads)
+    value, steps, wall = oracle_processes(n, 1000, 1, seconds, nproc, threads=threads)
     O.set_threads(1)
     V = I.initial_state(32, perturb=1e-3, seed=1)
     k, t1 = 0, time.perf_counter()
@@ -222,18 +223,19 @@ def cpu_baseline(n: int, seconds: float):
         e1 = time.perf_counter() - t1
         if e1 >= 1.0 or k >= 50:
             break
-    return {"value": value, "unit": "cell-updates/s", "cores": nproc, "cpu_model": cpu_model(), "kind": "port",
-            "sample": f"{nproc} single-threaded processes, {steps} RK3 steps in all of their own {n}^3 boxes, "
-                      f"{wall:.1f} s", "one_core_32": 32 ** 3 * k / e1}
+    return {"value": value, "unit": "cell-updates/s", "cores": nproc * threads, "cpu_model": cpu_model(),
+            "kind": "port", "sample": f"{nproc} processes x {threads} threads, {steps} RK3 steps in all of their own "
+                                      f"{n}^3 boxes, {wall:.1f} s", "one_core_32": 32 ** 3 * k / e1}
 
 
-def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
-    """One single-threaded run of the reference algorithm (a child process of oracle_processes):
-    `warmup` untimed steps, a barrier with the other processes, then up to `steps` timed steps or
-    `seconds` of them.  Puts the steps done and the wall-clock start and end of the timed part."""
+def _oracle_process(n, steps, warmup, seconds, which, threads, barrier, out):
+    """One run of the reference algorithm (a child process of oracle_processes) on `threads`
+    threads: `warmup` untimed steps, a barrier with the other processes, then up to `steps` timed
+    steps or `seconds` of them.  Puts the steps done and the wall-clock start and end of the timed
+    part."""
     from cns_nospec_gb300 import initdata as I
     from oracle import oracle as O
-    O.set_threads(1)
+    O.set_threads(threads)
     U = I.initial_state(n, perturb=1e-3, seed=1)
     dx = I.box_dx(n)
     for _ in range(warmup):
@@ -248,11 +250,11 @@ def _oracle_process(n, steps, warmup, seconds, which, barrier, out):
     out.put((k, t0, time.time()))
 
 
-def host_processes(n: int) -> int:
-    """Processes for oracle_processes: one per host core, but no more than half of the host's
-    memory holds (an n^3 oracle step holds about 34 doubles per ghost-inclusive cell: U, Unew,
-    Q, D, F and diffterm's nine temporaries)."""
-    cores = os.cpu_count() or 1
+def host_processes(n: int, threads: int = 1) -> int:
+    """Processes for oracle_processes: one per `threads` host cores, but no more than half of the
+    host's memory holds (an n^3 oracle step holds about 34 doubles per ghost-inclusive cell: U,
+    Unew, Q, D, F and diffterm's nine temporaries)."""
+    cores = max(1, (os.cpu_count() or 1) // threads)
     try:
         mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
     except (ValueError, OSError, AttributeError):
@@ -261,16 +263,26 @@ def host_processes(n: int) -> int:
     return max(1, min(cores, int(mem // 2 // per)))
 
 
-def oracle_processes(n, steps, warmup, seconds, nproc, which="port"):
-    """The reference algorithm on every host core the way its single-threaded cpu/ code uses
-    them: `nproc` independent processes (spawned), each advancing its own copy of the n^3 box,
-    their timed parts started together.  Throughput = all processes' cell-updates / (last end -
-    first start).  Returns (throughput, steps done in all, wall seconds)."""
+def host_split(which: str) -> int:
+    """Threads per process for the reference algorithm on the host cores.  The reference's
+    own cpu/ objects are single-threaded: one process per core.  The port threads its loops
+    (OpenMP): two threads per process, which on the 16 Neoverse-V2 cores of a GB300 host gives the
+    throughput of 16 single-threaded processes (1.69e7 cell-updates/s at 256^3 either way) in half
+    the time per step (7.9 s against 15.9 s), where 4 x 4 gave 1.64e7 and 1 x 16 1.37e7."""
+    threads = 2 if which == "port" and (os.cpu_count() or 1) >= 2 else 1
+    return threads
+
+
+def oracle_processes(n, steps, warmup, seconds, nproc, which="port", threads=1):
+    """The reference algorithm on the host cores: `nproc` independent processes (spawned) of
+    `threads` threads each, each advancing its own copy of the n^3 box, their timed parts started
+    together.  Throughput = all processes' cell-updates / (last end - first start).  Returns
+    (throughput, steps done in all, wall seconds)."""
     import multiprocessing as mp
     import queue
     ctx = mp.get_context("spawn")
     barrier, out = ctx.Barrier(nproc), ctx.Queue()
-    procs = [ctx.Process(target=_oracle_process, args=(n, steps, warmup, seconds, which, barrier, out))
+    procs = [ctx.Process(target=_oracle_process, args=(n, steps, warmup, seconds, which, threads, barrier, out))
              for _ in range(nproc)]
     for p in procs:
         p.start()
@@ -327,9 +339,9 @@ def run_reference(args, dist):
     the same warm-up and timed step counts as the GPU arm.  Where the reference tree exists its
     own cpu/ objects run (oracle/_ref); elsewhere (where it is absent and x86 objects do not
     travel) the oracle port, which gives the same bits.  Its cpu/ path is single-threaded, so it
-    uses the cores as one process per core, each advancing its own copy of the box
-    (oracle_processes): `warmup` untimed steps each, then `steps` timed steps each (a step of
-    this arm: every process advances its box one RK3 step), bounded to 20 minutes."""
+    uses the cores as independent processes, each advancing its own copy of the box (host_split,
+    oracle_processes): `warmup` untimed steps each, then `steps` timed steps each (a step of this
+    arm: every process advances its box one RK3 step), bounded to 20 minutes."""
     if dist.rank != 0:
         return None
     from oracle import oracle as O
@@ -337,18 +349,19 @@ def run_reference(args, dist):
     use_ref = O.have_ref() and os.path.isdir(O.REF_SRC)
     which = "ref" if use_ref else "port"
     n = args.n
-    procs = host_processes(n)
-    v, done, wall = oracle_processes(n, args.steps, args.warmup, 1200.0, procs, which=which)
+    threads = host_split(which)
+    procs = host_processes(n, threads)
+    v, done, wall = oracle_processes(n, args.steps, args.warmup, 1200.0, procs, which=which, threads=threads)
     steps = max(1, done // procs)
     kind = "reference" if use_ref else "port"
-    sample = (f"{procs} single-threaded processes x ({args.warmup} untimed + {steps} timed) RK3 steps of their own "
-              f"{n}^3 box, {wall:.1f} s timed")
+    sample = (f"{procs} processes x {threads} threads, each ({args.warmup} untimed + {steps} timed) RK3 steps of "
+              f"its own {n}^3 box, {wall:.1f} s timed")
     return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(n),
-            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": procs, "cpu_model": cpu_model(), "kind": kind,
-                             "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": procs * threads, "cpu_model": cpu_model(),
+                             "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
