@@ -81,6 +81,17 @@ struct BoxScalars {
     // annihilates a constant, and the energy flux splits exactly as
     // d((E+p) u)/dx = H_ref du/dx + d(((E+p) - H_ref) u)/dx.
     double p_ref, e_ref, E_ref, H_ref;
+    // The plain form's fixed-point copies of the P sets (cns_exact.cuh): fx_bad[s] != 0 when the
+    // copy of P[s] is unusable (not written, or a value did not fit its exponent), fx_e[s][f] the
+    // exponent of field f in it; fx_prev[f] / fx_cur[f] the largest biased exponent field of P
+    // field f over the previous step's writes / the writes since.  fx_restore: the box was just
+    // restored with its exponents (the conversion after the upload keeps fx_e, and fx_prev stays).
+    int fx_bad[2];
+    int fx_restore;
+    int fx_pad;
+    int fx_e[2][NPF];
+    int fx_prev[NPF];
+    int fx_cur[NPF];
 };
 
 constexpr int DTLOG_CAP = 1024;
@@ -110,6 +121,9 @@ struct BoxView {
                             // (256 threads, one cell each, k fastest across a warp)
     CoefT<double> c64;
     CoefT<float> c32;
+    long long* X[2];        // plain FP64 boxes: fixed-point copies of P[0], P[1] (NPF fields each,
+                            // the P sets' geometry); null for mixed boxes
+    int fx;                 // the box's assembly reads the fixed-point copies (CNS_ASSEMBLE_TMA_FX)
 };
 
 // A unit of work: one tile of one box, with origin (i0, j0, k0); its shape is the box's tlog.

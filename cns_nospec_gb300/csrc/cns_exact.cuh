@@ -196,6 +196,76 @@ __host__ __device__ __forceinline__ double xd2acc_nb(double acc, const Ld& ld, c
     return fma(b[4], x, acc);
 }
 
+// ---- fixed-point copies of the stencil fields ------------------------------------------------
+// The integer sums above place each tap's significand for every stencil that reads it (~20
+// integer instructions a tap).  The plain form's TMA-staged assembly instead reads a fixed-point
+// copy of each field its stencils read: X = trunc(v * 2^-E), one exponent E per field and box,
+// chosen so that |X| < 2^62, stored as two 31-bit chunks in one 64-bit word (low word X mod 2^31,
+// in [0, 2^31); high word X >> 31, signed).  A stencil is then two wide integer multiply-adds per
+// tap, with no placement, and S = sum_m w_m X_m is exact in two 64-bit accumulators (|w| sums to
+// at most 18418 < 2^15); it is rounded once to FP64 (xround) as S * 2^E.  Against the exact sum
+// sum_m w_m v_m the result is within half an ulp of itself plus sum|w| * 2^E: with E set from the
+// field's largest magnitude M (M < 2^(E + 60)), within sum|w| * 2^-60 M.  The producer of a field
+// writes its copy; values that do not fit (|v| >= 2^(E + 62) by the exponent test, or not finite)
+// are reported, and the assembly then reads the FP64 fields instead.
+constexpr int kFxHeadroom = 1082;  // E = (biased exponent field of M) - 1082: M < 2^(E + 60)
+
+// E for a field whose largest biased exponent field was emax (0 when every value was zero).
+__host__ __device__ __forceinline__ int fx_exponent(int emax) { return (emax > 0 ? emax : 1) - kFxHeadroom; }
+
+// The fixed-point word of v at exponent E; *bad set when it does not fit.
+__host__ __device__ __forceinline__ long long fx_word(double v, int E, bool* bad) {
+    const int hi = xhi(v);
+    const int e = (hi >> 20) & 0x7FF;
+    const unsigned long long m = ((unsigned long long)(((unsigned)hi & 0xFFFFFu) | (e ? 0x100000u : 0u)) << 32) | xlo(v);
+    const int sh = (e > 1 ? e : 1) - 1075 - E;  // X = m * 2^sh, truncated toward zero
+    *bad |= (e == 0x7FF) | (sh > 9);
+    const int r = -sh < 63 ? -sh : 63;
+    const unsigned long long x = sh >= 0 ? (m << (sh & 15)) : (m >> r);  // < 2^62 unless bad
+    const long long X = (hi < 0) ? -(long long)x : (long long)x;
+    return (long long)(((unsigned long long)(unsigned)(int)(X >> 31) << 32) | (unsigned long long)(X & 0x7FFFFFFFll));
+}
+
+// Exponent field of |v| (bits 20-30 of its high word) for the producers' maxima.
+__host__ __device__ __forceinline__ int fx_efield(double v) { return (xhi(v) >> 20) & 0x7FF; }
+
+// One tap of weight wt into the accumulators.
+__host__ __device__ __forceinline__ void fx_tap(long long& L, long long& H, long long w, int wt) {
+    L += (long long)wt * (long long)(int)(unsigned)(w & 0xFFFFFFFFll);
+    H += (long long)wt * (long long)(int)(w >> 32);
+}
+
+// sum_{m=1..4} w_m (X(m) + SGN X(-m)) of fixed-point words, rounded once to FP64 and scaled by
+// 2^E; false when the result is outside FP64's normal range (then *out is unspecified).
+template <int W1, int W2, int W3, int W4, int SGN, class Ld>
+__host__ __device__ __forceinline__ bool fx_sum8(const Ld& ld, int E, double* out) {
+    long long L = 0, H = 0;
+    fx_tap(L, H, ld(1), W1);
+    fx_tap(L, H, ld(-1), SGN * W1);
+    fx_tap(L, H, ld(2), W2);
+    fx_tap(L, H, ld(-2), SGN * W2);
+    fx_tap(L, H, ld(3), W3);
+    fx_tap(L, H, ld(-3), SGN * W3);
+    fx_tap(L, H, ld(4), W4);
+    fx_tap(L, H, ld(-4), SGN * W4);
+    return xround(H, L, E, out);
+}
+
+// First / second derivative stencils on fixed-point words: acc + a[4] * sum, *fail where the sum
+// is outside FP64's normal range.
+template <class Ld>
+__host__ __device__ __forceinline__ double fx_d1acc(double acc, const Ld& ld, int E, const double* a, bool* fail) {
+    double x;
+    *fail |= !fx_sum8<672, -168, 32, -3, -1>(ld, E, &x);
+    return fma(a[4], x, acc);
+}
+template <class Ld>
+__host__ __device__ __forceinline__ double fx_d2acc(double acc, const Ld& ld, int E, const double* b, bool* fail) {
+    double x;
+    *fail |= !fx_sum8<8064, -1008, 128, -9, 1>(ld, E, &x);
+    return fma(b[4], x, acc);
+}
+
 // Tap loaders: a strided array (global memory through a chosen load, or shared memory) and a
 // register column.
 template <int MODE>  // 0: read-only path, 1: L2 (data written during the launch), 2: plain
