@@ -97,6 +97,7 @@ struct Geometry {
     long long sj, si, fs;
     size_t off_sc, off_dtlog, off_U, off_Us, off_P0, off_P1, off_S, off_view, off_tiles, off_aos, total;
     size_t off_xtiles, off_maps;  // mixed boxes: TMA-assembly tiles and tensor maps
+    size_t off_X0, off_X1;        // plain FP64 boxes: fixed-point copies of the P sets (else 0)
     int ntiles;                   // capacity of the tile list (largest candidate shape)
     int nxtiles;                  // TMA-assembly tiles (8 x 8 x 32 cells)
 };
@@ -173,6 +174,11 @@ static Geometry geometry(const cns_box_desc* d) {
     g.off_P0 = o;      o = align256(o + esz * NPF * g.fs);
     g.off_P1 = o;      o = align256(o + esz * NPF * g.fs);
     g.off_S = o;       o = align256(o + esz * NSF * g.fs);
+    g.off_X0 = g.off_X1 = 0;
+    if (d->precision == CNS_FP64) {
+        g.off_X0 = o;  o = align256(o + sizeof(long long) * NPF * g.fs);
+        g.off_X1 = o;  o = align256(o + sizeof(long long) * NPF * g.fs);
+    }
     g.off_view = o;    o = align256(o + sizeof(BoxView));
     g.off_tiles = o;   o = align256(o + sizeof(Tile) * g.ntiles);
     g.off_aos = o;     o = align256(o + sizeof(double) * CNS_NC * g0 * g1 * g2);
@@ -313,6 +319,10 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     v.dtlog = (double*)(b->arena + g.off_dtlog);
     v.cfl = desc->cfl;
     v.precision = desc->precision;
+    if (desc->precision == CNS_FP64) {
+        v.X[0] = (long long*)(b->arena + g.off_X0);
+        v.X[1] = (long long*)(b->arena + g.off_X1);
+    }
     fill_coefs(v, desc);
     b->d_view = (BoxView*)(b->arena + g.off_view);
     b->d_tiles = (Tile*)(b->arena + g.off_tiles);
@@ -394,7 +404,17 @@ extern "C" int cns_box_set_stream(cns_box* b, void* stream) {
 // Prime a box whose U interior was just written: primitives/fluxes, Courant, first dt.
 // `restore` (a snapshot's scalars) keeps its step count and reference values instead of
 // deriving fresh ones, so a resumed run continues bit for bit.
+// The plain form's fixed-point copy of the P set an upload just wrote (boxes on
+// CNS_ASSEMBLE_TMA_FX): its fields' maxima (unless restored exponents are kept), then the copy.
+static int fx_after_upload(cns_box* b, bool restored) {
+    if (!b->view.fx) return CNS_OK;
+    if (!restored) CK(launch_fx_pass(false, b->d_view, b->d_tiles, b->ntiles, b->stream));
+    CK(launch_fx_pass(true, b->d_view, b->d_tiles, b->ntiles, b->stream));
+    return CNS_OK;
+}
+
 static int prime(cns_box* b, const BoxScalars* restore = nullptr) {
+    bool fx_restored = false;  // a restore whose saved fixed-point copy was usable keeps its exponents
     if (restore) {
         BoxScalars s;
         memset(&s, 0, sizeof s);
@@ -404,6 +424,14 @@ static int prime(cns_box* b, const BoxScalars* restore = nullptr) {
         s.e_ref = restore->e_ref;
         s.E_ref = restore->E_ref;
         s.H_ref = restore->H_ref;
+        // the saved P set becomes P[0]: its copy is made again at the saved exponents, and the next
+        // writes take theirs from the saved maxima, so the run continues bit for bit
+        fx_restored = b->view.fx && !restore->fx_bad[restore->pbase & 1];
+        s.fx_restore = fx_restored ? 1 : 0;
+        for (int f = 0; f < NPF && fx_restored; f++) {
+            s.fx_e[0][f] = restore->fx_e[restore->pbase & 1][f];
+            s.fx_prev[f] = restore->fx_prev[f];
+        }
         CK(cudaMemcpyAsync(b->d_sc, &s, sizeof s, cudaMemcpyHostToDevice, b->stream));
         CK(cudaStreamSynchronize(b->stream));  // s lives on this stack frame
     } else {
@@ -411,6 +439,8 @@ static int prime(cns_box* b, const BoxScalars* restore = nullptr) {
         CK(launch_refs(b->d_view, 1, b->stream));
     }
     CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->ntiles, b->stream));
+    int rc = fx_after_upload(b, fx_restored);
+    if (rc) return rc;
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return CNS_OK;
@@ -450,6 +480,8 @@ static int upload_host(cns_box* b, const double* U_host, double* h_map, bool gho
     CK(host_upload(b->view, h_map, fp64, ghosts, b->stream));
     CK(launch_refs(b->d_view, 1, b->stream));
     if (!fp64) CK(launch_prim(b->desc.precision, b->d_view, b->d_tiles, b->ntiles, b->stream));
+    int rc = fx_after_upload(b, false);
+    if (rc) return rc;
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return CNS_OK;
@@ -512,6 +544,8 @@ struct WorkLists {
     int nw32 = 0;
     const Tile* dx32 = nullptr;  // the derivative pass of mixed boxes on either TMA assembly
     int ndx32 = 0;
+    const Tile* f64 = nullptr;  // FP64 boxes on the fixed-point TMA assembly
+    int nf64 = 0;
 };
 
 // One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
@@ -551,6 +585,10 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
             CK(launch_assemble_tma64(views, w.x64, w.nx64, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
+        if (w.nf64) {
+            CK(launch_assemble_fx(views, w.f64, w.nf64, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
         if (w.na32) {
             CK(launch_assemble(1, views, w.a32, w.na32, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
@@ -581,6 +619,8 @@ static WorkLists box_lists(const cns_box* b) {
         w.d64 = b->d_tiles, w.nd64 = b->ntiles;
         if (b->kernel == CNS_ASSEMBLE_TMA)
             w.x64 = b->d_xtiles, w.nx64 = b->nxtiles;
+        else if (b->kernel == CNS_ASSEMBLE_TMA_FX)
+            w.f64 = b->d_xtiles, w.nf64 = b->nxtiles;
         else
             w.a64 = b->d_tiles, w.na64 = b->ntiles;
     }
@@ -817,12 +857,17 @@ extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->member
 static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
-    std::vector<Tile> d64, d32, a32, x32, w32, dx32;  // the lists of WorkLists
+    std::vector<Tile> d64, a64, f64, d32, a32, x32, w32, dx32;  // the lists of WorkLists
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
         if (b->desc.precision != CNS_MIXED) {
+            // FP64 members: the direct assembly, or the fixed-point TMA one
             append_tiles(b->desc.n, b->view.tlog, (int)m, d64);
+            if (b->kernel == CNS_ASSEMBLE_TMA_FX)
+                append_xtiles(b->desc.n, (int)m, f64);
+            else
+                append_tiles(b->desc.n, b->view.tlog, (int)m, a64);
             continue;
         }
         if (b->kernel == CNS_ASSEMBLE_TMA || b->kernel == CNS_ASSEMBLE_TMA_WS) {
@@ -834,8 +879,8 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
         }
     }
     std::vector<Tile> all;
-    all.reserve(d64.size() + d32.size() + a32.size() + x32.size() + w32.size() + dx32.size());
-    for (auto* v : {&d64, &d32, &a32, &x32, &w32, &dx32}) all.insert(all.end(), v->begin(), v->end());
+    all.reserve(d64.size() + a64.size() + f64.size() + d32.size() + a32.size() + x32.size() + w32.size() + dx32.size());
+    for (auto* v : {&d64, &a64, &f64, &d32, &a32, &x32, &w32, &dx32}) all.insert(all.end(), v->begin(), v->end());
     const size_t nt = all.size();
     if (views.size() > bt->cap_views) {
         cudaFree(bt->d_views);
@@ -854,7 +899,9 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     WorkLists& w = bt->lists;
     w = WorkLists();
     Tile* at = bt->d_tiles;
-    w.d64 = w.a64 = at, w.nd64 = w.na64 = (int)d64.size(), at += d64.size();  // FP64: direct assembly
+    w.d64 = at, w.nd64 = (int)d64.size(), at += d64.size();
+    w.a64 = at, w.na64 = (int)a64.size(), at += a64.size();
+    w.f64 = at, w.nf64 = (int)f64.size(), at += f64.size();
     w.d32 = at, w.nd32 = (int)d32.size(), at += d32.size();
     w.a32 = at, w.na32 = (int)a32.size(), at += a32.size();
     w.x32 = at, w.nx32 = (int)x32.size(), at += x32.size();
@@ -1137,6 +1184,8 @@ static int upload_first_step(cns_box* b, double* h_map, bool ghosts) {
     CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
     CK(host_upload_deriv(b->view, h_map, ghosts, b->d_tiles, b->d_queue, b->nq, b->d_counters, b->stream));
     // (no k_refs: the FP64 form does not use the mixed form's reference values)
+    int rc = fx_after_upload(b, false);
+    if (rc) return rc;
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return enqueue_step(b->d_view, 1, box_lists(b), b->stream, nullptr, nullptr, true);
@@ -1255,6 +1304,9 @@ struct SnapHeader {
     double dx[3], cfl, eta, alam;
     double p_ref, e_ref, E_ref, H_ref, dt_last;
     int64_t payload_doubles;
+    // version 2: the fixed-point exponents of the saved P set and the maxima the next writes take
+    // theirs from (fx_valid = 0: none; they are derived again at load)
+    int32_t fx_valid, fx_e[NPF], fx_prev[NPF];
 };
 
 extern "C" int cns_box_save(cns_box* b, const char* path) {
@@ -1269,7 +1321,7 @@ extern "C" int cns_box_save(cns_box* b, const char* path) {
     SnapHeader h;
     memset(&h, 0, sizeof h);
     memcpy(h.magic, "CNSSNAP1", 8);
-    h.version = 1;
+    h.version = 2;
     h.precision = b->desc.precision;
     for (int a = 0; a < 3; a++) {
         h.n[a] = b->desc.n[a];
@@ -1286,6 +1338,11 @@ extern "C" int cns_box_save(cns_box* b, const char* path) {
     h.H_ref = hs.H_ref;
     h.dt_last = hs.dt_last;
     h.payload_doubles = (int64_t)U.size();
+    h.fx_valid = (b->view.fx && !hs.fx_bad[hs.pbase & 1]) ? 1 : 0;
+    for (int q = 0; q < NPF; q++) {
+        h.fx_e[q] = hs.fx_e[hs.pbase & 1][q];
+        h.fx_prev[q] = hs.fx_prev[q];
+    }
     FILE* f = fopen(path, "wb");
     if (!f) return fail(CNS_ERR_INVALID, "cannot create %s", path);
     bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(U.data(), sizeof(double), U.size(), f) == U.size();
@@ -1300,7 +1357,12 @@ extern "C" int cns_box_load(cns_box* b, const char* path) {
     if (!f) return fail(CNS_ERR_INVALID, "cannot open %s", path);
     SnapHeader h;
     std::vector<double> U(aos_bytes(b) / sizeof(double));
-    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "CNSSNAP1", 8) == 0 && h.version == 1;
+    // version 1 headers end before the fixed-point fields
+    const size_t v1_bytes = offsetof(SnapHeader, fx_valid);
+    memset(&h, 0, sizeof h);
+    bool ok = fread(&h, v1_bytes, 1, f) == 1 && memcmp(h.magic, "CNSSNAP1", 8) == 0 &&
+              (h.version == 1 || h.version == 2);
+    if (ok && h.version == 2) ok = fread((char*)&h + v1_bytes, sizeof h - v1_bytes, 1, f) == 1;
     if (ok) {
         ok = h.precision == b->desc.precision && h.ng == CNS_NG && h.payload_doubles == (int64_t)U.size();
         for (int a = 0; a < 3; a++) ok = ok && h.n[a] == b->desc.n[a] && h.dx[a] == b->desc.dx[a];
@@ -1323,6 +1385,12 @@ extern "C" int cns_box_load(cns_box* b, const char* path) {
     s.e_ref = h.e_ref;
     s.E_ref = h.E_ref;
     s.H_ref = h.H_ref;
+    s.pbase = 0;
+    s.fx_bad[0] = h.fx_valid ? 0 : 1;
+    for (int q = 0; q < NPF; q++) {
+        s.fx_e[0][q] = h.fx_e[q];
+        s.fx_prev[q] = h.fx_prev[q];
+    }
     int rc = prime(b, &s);
     if (rc) return rc;
     CK(cudaStreamSynchronize(b->stream));
@@ -1383,9 +1451,36 @@ static int restore_state(cns_box* b, const BoxScalars* hs) {
     return prime(b, hs);
 }
 
+// A box on CNS_ASSEMBLE_TMA_FX keeps the fixed-point copy of the P set it reads (view.fx); on
+// any other kernel the copies are neither written nor read.  Switching onto it between steps
+// makes the copy of the current P set at once (maxima, then the copy) and takes those maxima for
+// the next writes.
+static int push_fx(cns_box* b) {
+    const int fx = (b->desc.precision == CNS_FP64 && b->kernel == CNS_ASSEMBLE_TMA_FX) ? 1 : 0;
+    if (fx == b->view.fx) return CNS_OK;
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
+    b->view.fx = fx;
+    static const int kNone[2] = {0, 0}, kBoth[2] = {1, 1};
+    CK(cudaMemcpyAsync(&b->d_sc->fx_bad[0], fx ? kNone : kBoth, sizeof kBoth, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, fx), &b->view.fx, sizeof(int), cudaMemcpyHostToDevice,
+                       b->stream));
+    if (fx && b->primed) {
+        int rc = fx_after_upload(b, false);
+        if (rc) return rc;
+        CK(launch_fx_adopt(b->d_view, 1, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->batch) b->batch->dirty = true;
+    return CNS_OK;
+}
+
 static int apply_kernel(cns_box* b, int kernel) {
-    if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA && kernel != CNS_ASSEMBLE_TMA_WS)
+    if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA && kernel != CNS_ASSEMBLE_TMA_WS &&
+        kernel != CNS_ASSEMBLE_TMA_FX)
         return fail(CNS_ERR_INVALID, "unknown kernel %d", kernel);
+    if (kernel == CNS_ASSEMBLE_TMA_FX && b->desc.precision != CNS_FP64)
+        return fail(CNS_ERR_INVALID, "the fixed-point TMA assembly serves plain FP64 boxes only");
     if (kernel != CNS_ASSEMBLE_DIRECT && !b->view.tma)
         return fail(CNS_ERR_INVALID, "the TMA assemblies need the box's tensor maps");
     if (kernel == CNS_ASSEMBLE_TMA_WS && b->desc.precision != CNS_MIXED)
@@ -1399,7 +1494,7 @@ static int apply_kernel(cns_box* b, int kernel) {
         b->gexec = nullptr;
     }
     if (b->batch) b->batch->dirty = true;
-    return CNS_OK;
+    return push_fx(b);
 }
 
 extern "C" int cns_box_get_kernel(const cns_box* b, int* kernel) {
@@ -1427,10 +1522,13 @@ extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], in
     // one block per SM, measured 23 % slower on GB300, is an explicit option)
     const int nkern = (b->desc.precision == CNS_MIXED && b->view.tma) ? 3 : 1;
     int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]}, best_k = b->kernel;
+    // FP64 boxes keep their arithmetic: on the fixed-point TMA assembly (8x8x32 tiles, nothing to
+    // tune but the derivative pass's shape) only the derivative pass's shapes are tried
+    const bool keep_fx = b->kernel == CNS_ASSEMBLE_TMA_FX;
     double best_t = 1e300;
     for (int c = -1; c < nkern * kNumShapes; c++) {  // c = -1: a warm-up trial, not scored
         const int* t = kShapes[c < 0 ? 0 : c % kNumShapes];
-        const int k = c < 0 ? b->kernel : c / kNumShapes;
+        const int k = (c < 0 || keep_fx) ? b->kernel : c / kNumShapes;
         if ((rc = apply_tile(b, t)) || (rc = apply_kernel(b, k))) return rc;
         double ms = 0.0;
         if ((rc = timed_run(b->stream, trial_steps, b->d_view, 1, box_lists(b), nullptr, nullptr, &ms))) return rc;

@@ -43,6 +43,8 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __rest
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
+        // the assembly after this kernel writes the other P set (and its fixed-point copy)
+        if (sizeof(R) == 8) fx_prepare(b, b.sc->pbase ^ ((stage - 1) & 1) ^ 1);
         int i, j, k;
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
         if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
@@ -179,6 +181,59 @@ __global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int fli
     }
     s->dt = boxes[bx].cfl / courno;
     s->courno_bits = 0ull;
+    // The plain form's fixed-point exponents: the next step's writes take them from the maxima of
+    // this step's writes (after an upload, of the uploaded P set; after a restore, the restored ones)
+    if (flip || !s->fx_restore) {
+        for (int f = 0; f < NPF; f++) s->fx_prev[f] = s->fx_cur[f];
+    }
+    for (int f = 0; f < NPF; f++) s->fx_cur[f] = 0;
+    s->fx_restore = 0;
+    fx_prepare_one(boxes[bx], s->pbase ^ 1);  // written by the next stage 1 (whose derivative pass
+                                              // may ride with an upload)
+}
+
+// ---- k_fx_pass: the fixed-point copy of a box's uploaded P set ------------------------------
+// CONVERT = false: the maxima of the P set's fields into fx_cur (a fresh upload).  CONVERT = true:
+// the copy at exponents from those maxima, or, after a restore, at the restored exponents.
+template <bool CONVERT>
+__global__ void __launch_bounds__(kTileThreads) k_fx_pass(const BoxView* __restrict__ boxes,
+                                                        const Tile* __restrict__ tiles, int ntiles) {
+    __shared__ int s_emax[NPF];
+    if (threadIdx.x < NPF) s_emax[threadIdx.x] = 0;
+    __syncthreads();
+    int fx_box = -1, fx_set = 0;
+    bool bad = false;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const Tile T = tiles[t];
+        const BoxView& b = boxes[T.box];
+        BoxScalars* sc = b.sc;
+        const int W = sc->pbase;
+        if (T.box != fx_box) {
+            fx_flush(boxes, fx_box, fx_set, s_emax, bad);
+            bad = false;
+            fx_box = T.box;
+            fx_set = W;
+            if (CONVERT && !sc->fx_restore && threadIdx.x < NPF)
+                sc->fx_e[W][threadIdx.x] = fx_exponent(sc->fx_cur[threadIdx.x]);
+        }
+        int i, j, k;
+        tile_pos(b, T, threadIdx.x, &i, &j, &k);
+        if (i < b.n[0] && j < b.n[1] && k < b.n[2]) {
+            const double* P = (const double*)b.P[W];
+            const long long c = cell_off(b, i, j, k);
+#pragma unroll
+            for (int f = 0; f < NPF; f++) {
+                const double v = P[f * b.fs + c];
+                if (!CONVERT) {
+                    fx_track(s_emax + f, fx_efield(v));
+                } else {
+                    const int E = sc->fx_restore ? sc->fx_e[W][f] : fx_exponent(sc->fx_cur[f]);
+                    store_img(b.X[W] + f * b.fs, b, c, i, j, k, fx_word(v, E, &bad), pimg(f));
+                }
+            }
+        }
+    }
+    fx_flush(boxes, fx_box, fx_set, s_emax, bad);
 }
 
 // ---- launch helpers ---------------------------------------------------------------------
@@ -237,6 +292,31 @@ cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* til
 cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st) {
     if (nboxes <= 0) return cudaSuccess;
     k_refs<<<(nboxes + 127) / 128, 128, 0, st>>>(boxes, nboxes);
+    return cudaGetLastError();
+}
+// ---- k_fx_adopt: a box switched onto its fixed-point copies between steps takes the maxima of
+// the conversion just made for its next writes (k_stepend's bookkeeping without a step)
+__global__ void k_fx_adopt(const BoxView* __restrict__ boxes, int nboxes) {
+    const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bx >= nboxes) return;
+    BoxScalars* s = boxes[bx].sc;
+    for (int f = 0; f < NPF; f++) {
+        s->fx_prev[f] = s->fx_cur[f];
+        s->fx_cur[f] = 0;
+    }
+    fx_prepare_one(boxes[bx], s->pbase ^ 1);
+}
+cudaError_t launch_fx_adopt(const BoxView* boxes, int nboxes, cudaStream_t st) {
+    if (nboxes <= 0) return cudaSuccess;
+    k_fx_adopt<<<(nboxes + 127) / 128, 128, 0, st>>>(boxes, nboxes);
+    return cudaGetLastError();
+}
+cudaError_t launch_fx_pass(bool convert, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (convert)
+        k_fx_pass<true><<<grid_for((const void*)k_fx_pass<true>, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
+    else
+        k_fx_pass<false><<<grid_for((const void*)k_fx_pass<false>, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
     return cudaGetLastError();
 }
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st) {

@@ -301,6 +301,60 @@ __device__ __forceinline__ int health_bits(double rho, double eint) {
     return h;
 }
 
+// ---- the plain form's fixed-point copies (cns_exact.cuh) ------------------------------------
+// Largest exponent field of each P field over a block's writes: a warp maximum, folded into the
+// block's shared slot by the lowest active lane (the callers run in divergent code).
+__device__ __forceinline__ void fx_track(int* slot, int efield) {
+    const unsigned mask = __activemask();
+    const int m = (int)__reduce_max_sync(mask, (unsigned)efield);
+    if ((mask & ((1u << (threadIdx.x & 31)) - 1u)) == 0) atomicMax(slot, m);
+}
+
+// Where the plain form's write-back also puts the fixed-point copy of the P set it writes: the
+// copy, its exponents, the block's shared maxima, and whether a value did not fit.
+struct FxSink {
+    long long* X;
+    const int* E;
+    int* s_emax;
+    bool bad;
+};
+__device__ __forceinline__ void fx_store(FxSink& fx, const BoxView& b, long long c, int i, int j, int k, int f,
+                                         double v, int mask) {
+    const long long w = fx_word(v, fx.E[f], &fx.bad);
+    store_img(fx.X + f * b.fs, b, c, i, j, k, w, mask);
+    fx_track(fx.s_emax + f, fx_efield(v));
+}
+
+// The block's maxima and overflow for box `bx` (set W written) into the box's scalars, and the
+// slots cleared.  Every thread of the block calls it (block barriers).
+__device__ __forceinline__ void fx_flush(const BoxView* boxes, int bx, int W, int* s_emax, bool bad) {
+    const int any_bad = __syncthreads_or(bad ? 1 : 0);
+    if (bx >= 0) {
+        BoxScalars* sc = boxes[bx].sc;
+        if (threadIdx.x < NPF && s_emax[threadIdx.x] > 0) atomicMax(&sc->fx_cur[threadIdx.x], s_emax[threadIdx.x]);
+        if (threadIdx.x == 0 && any_bad) atomicOr(&sc->fx_bad[W], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < NPF) s_emax[threadIdx.x] = 0;
+    __syncthreads();
+}
+
+// Prepares the write of set W by the next kernel (the assembly after a derivative pass): its
+// exponents from the previous step's maxima, usable unless a value overflows (boxes whose
+// assembly reads the FP64 fields: never usable).  Threads 0..NPF of the caller store (the same
+// values from every block).
+// The same from one thread (k_stepend).
+__device__ __forceinline__ void fx_prepare_one(const BoxView& b, int W) {
+    BoxScalars* sc = b.sc;
+    for (int f = 0; f < NPF; f++) sc->fx_e[W][f] = fx_exponent(sc->fx_prev[f]);
+    sc->fx_bad[W] = b.fx ? 0 : 1;
+}
+__device__ __forceinline__ void fx_prepare(const BoxView& b, int W) {
+    BoxScalars* sc = b.sc;
+    if (threadIdx.x < NPF) sc->fx_e[W][threadIdx.x] = fx_exponent(sc->fx_prev[threadIdx.x]);
+    if (threadIdx.x == NPF) sc->fx_bad[W] = b.fx ? 0 : 1;
+}
+
 // ctoprim + flux functions of one cell's FP64 conserved state, written to the P set `Pw`
 // with the periodic face images each field's stencils need.  Returns the cell's Courant
 // number (only formed when `want_cour`).  Plain form: everything in FP64 (reciprocal by
@@ -358,9 +412,11 @@ __device__ __forceinline__ float courant_plain_est(const BoxView& b, const Coura
     return fmaxf(fmaxf(cx, cy), cz);
 }
 
-// The plain form's epilogue without the Courant number, whose inputs it leaves in *q.
+// The plain form's epilogue without the Courant number, whose inputs it leaves in *q; with `fx`,
+// also the fixed-point copy of the P set it writes.
 __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restrict__ Pw, long long c, int i, int j,
-                                               int k, const double un[5], int* health, CourantInput64* q);
+                                               int k, const double un[5], int* health, CourantInput64* q,
+                                               FxSink* fx = nullptr);
 template <>
 __device__ __forceinline__ double epilogue<double>(const BoxView& b, double* __restrict__ Pw, long long c, int i,
                                                    int j, int k, const double un[5], bool want_cour, int* health) {
@@ -369,7 +425,8 @@ __device__ __forceinline__ double epilogue<double>(const BoxView& b, double* __r
     return want_cour ? courant_plain(b, q) : 0.0;
 }
 __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restrict__ Pw, long long c, int i, int j,
-                                               int k, const double un[5], int* health, CourantInput64* q) {
+                                               int k, const double un[5], int* health, CourantInput64* q,
+                                               FxSink* fx) {
     const long long fs = b.fs;
     const double rho = un[0], mx = un[1], my = un[2], mz = un[3], E = un[4];
     const double rinv = rcp_nr(rho);
@@ -383,22 +440,26 @@ __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restr
     *health |= health_bits(rho, eint);
     // Field by field, not store_pset: its 16 live FP64 values would cost the upload kernels
     // occupancy, and the FP64-bound kernels gain nothing from fewer store instructions.
-    store_img(Pw + PU * fs, b, c, i, j, k, u, 7);
-    store_img(Pw + PV * fs, b, c, i, j, k, v, 7);
-    store_img(Pw + PW * fs, b, c, i, j, k, w, 7);
-    store_img(Pw + PT * fs, b, c, i, j, k, eint, 7);
-    store_img(Pw + PMX * fs, b, c, i, j, k, mx, 1);
-    store_img(Pw + PMY * fs, b, c, i, j, k, my, 2);
-    store_img(Pw + PMZ * fs, b, c, i, j, k, mz, 4);
-    store_img(Pw + PFUU * fs, b, c, i, j, k, fma(mx, u, p), 1);
-    store_img(Pw + PFVV * fs, b, c, i, j, k, fma(my, v, p), 2);
-    store_img(Pw + PFWW * fs, b, c, i, j, k, fma(mz, w, p), 4);
-    store_img(Pw + PFUV * fs, b, c, i, j, k, mx * v, 3);
-    store_img(Pw + PFUW * fs, b, c, i, j, k, mx * w, 5);
-    store_img(Pw + PFVW * fs, b, c, i, j, k, my * w, 6);
-    store_img(Pw + PHU * fs, b, c, i, j, k, H * u, 1);
-    store_img(Pw + PHV * fs, b, c, i, j, k, H * v, 2);
-    store_img(Pw + PHW * fs, b, c, i, j, k, H * w, 4);
+    auto put = [&](int f, double val, int mask) {
+        store_img(Pw + f * fs, b, c, i, j, k, val, mask);
+        if (fx) fx_store(*fx, b, c, i, j, k, f, val, mask);
+    };
+    put(PU, u, 7);
+    put(PV, v, 7);
+    put(PW, w, 7);
+    put(PT, eint, 7);
+    put(PMX, mx, 1);
+    put(PMY, my, 2);
+    put(PMZ, mz, 4);
+    put(PFUU, fma(mx, u, p), 1);
+    put(PFVV, fma(my, v, p), 2);
+    put(PFWW, fma(mz, w, p), 4);
+    put(PFUV, mx * v, 3);
+    put(PFUW, mx * w, 5);
+    put(PFVW, my * w, 6);
+    put(PHU, H * u, 1);
+    put(PHV, H * v, 2);
+    put(PHW, H * w, 4);
     *q = CourantInput64{p, rinv, u, v, w};
 }
 

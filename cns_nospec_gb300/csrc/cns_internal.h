@@ -34,6 +34,11 @@ cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles,
 cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
                             cudaStream_t st);
 cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st);
+// the plain form's fixed-point copy of an uploaded P set: its fields' maxima (convert = false),
+// then the copy (convert = true); k_fx_pass
+cudaError_t launch_fx_pass(bool convert, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st);
+// a box switched onto its fixed-point copies between steps: maxima of the conversion -> exponents
+cudaError_t launch_fx_adopt(const BoxView* boxes, int nboxes, cudaStream_t st);
 // the TMA-staged assembly of mixed boxes (cns_tma.cu)
 void tma_tile_shape(int* ti, int* tj, int* tk);
 size_t tma_maps_bytes();
@@ -42,6 +47,8 @@ cudaError_t bounded_wait_selftest(int* status);
 cudaError_t exact_sums_selftest(const double* taps, int n, double* sums, int* ok);
 cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 cudaError_t launch_assemble_tma64(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
+// FP64 boxes on their fixed-point copies, TMA-staged (k_assemble_fx)
+cudaError_t launch_assemble_fx(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 // the mixed form's derivative pass on the same tiles, TMA-staged (same bits as launch_deriv)
 cudaError_t launch_deriv_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 // the warp-specialised TMA assembly (same tiles, same bits): stencils and FP64 write-back overlap

@@ -33,6 +33,7 @@ constexpr int kBufElems = box_elems(BX_FULL);  // 10240 floats, the largest box
 struct TmaMaps {
     CUtensorMap p[2][7];
     CUtensorMap s[4];
+    CUtensorMap x[2][7];  // plain FP64 boxes: the fixed-point copies of P[0], P[1] (64-bit words)
 };
 static_assert(sizeof(CUtensorMap) == 128, "CUtensorMap is 128 bytes");
 
@@ -94,7 +95,7 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int 
 
 // Issue the copy of `L` for tile `tile` into `buf`, completing on `bar` (R: float for mixed
 // boxes, double for FP64 boxes, whose tensor maps are FP64).
-template <class R>
+template <class R, bool FX = false>
 __device__ __forceinline__ void issue_load(const BoxView* boxes, const Tile* tiles, int tile, const Load L, int flip,
                                            R* buf, uint64_t* bar) {
     const Tile T = tiles[tile];
@@ -102,7 +103,8 @@ __device__ __forceinline__ void issue_load(const BoxView* boxes, const Tile* til
     const TmaMaps* maps = (const TmaMaps*)b.tma;
     const CUtensorMap* map;
     if (L.set == 0) {
-        map = &maps->p[b.sc->pbase ^ flip][L.shape];  // stage s reads P[pbase ^ ((s-1)&1)]
+        // stage s reads P[pbase ^ ((s-1)&1)] (FX: its fixed-point copy)
+        map = FX ? &maps->x[b.sc->pbase ^ flip][L.shape] : &maps->p[b.sc->pbase ^ flip][L.shape];
     } else {
         const int si = L.shape == BX_I ? 0 : L.shape == BX_J ? 1 : L.shape == BX_K ? 2 : 3;
         map = &maps->s[si];
@@ -112,10 +114,10 @@ __device__ __forceinline__ void issue_load(const BoxView* boxes, const Tile* til
     tma_load(buf, map, T.k0 + CNS_NG - hk, T.j0 + CNS_NG - hj, T.i0 + CNS_NG - hi, L.field, bar);
 }
 // Load number g of this block in kSched (tile g / 20, entry g % 20).
-template <class R>
+template <class R, bool FX = false>
 __device__ __forceinline__ void issue(const BoxView* boxes, const Tile* tiles, int tile, int entry, int flip,
                                       R* buf, uint64_t* bar) {
-    issue_load(boxes, tiles, tile, kSched[entry], flip, buf, bar);
+    issue_load<R, FX>(boxes, tiles, tile, kSched[entry], flip, buf, bar);
 }
 
 // ---- per-field consumers (compile-time box extents) ----------------------------------------
@@ -532,7 +534,7 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
 // part (block barriers at stage 3).
 template <int STAGE>
 __device__ __forceinline__ void write_back_plain(const BoxView& b, const Tile& T, double* stash, int col, int tj,
-                                                 int tk) {
+                                                 int tk, FxSink* fx = nullptr) {
     const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
     double* Pw = (double*)b.P[pr ^ 1];
     const double dt = b.sc->dt;
@@ -563,7 +565,7 @@ __device__ __forceinline__ void write_back_plain(const BoxView& b, const Tile& T
         }
         if (STAGE == 3 && b.host_out) store_host(b, ic, j, k, un);
         CourantInput64 q;
-        epilogue_plain(b, Pw, c, ic, j, k, un, &health, &q);
+        epilogue_plain(b, Pw, c, ic, j, k, un, &health, &q, fx);
         if (STAGE == 3) {
             const float est = courant_plain_est(b, q);
             reinterpret_cast<float*>(stash + (i * 5 + 0) * kTileThreads + col)[0] = est;
@@ -668,6 +670,236 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(R) == 4 ? 2 : 1) k_assemb
             write_back_plain<STAGE>(b, T, stash, tid, tj, tk);
         __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
     }
+}
+
+// ---- the plain form on its fixed-point copies (CNS_ASSEMBLE_TMA_FX) -------------------------
+// k_assemble_tma's tiles, schedule and FP64 write-back, with the P fields staged as the 64-bit
+// fixed-point words of the stage's copy (cns_exact.cuh) instead of FP64: every Laplacian and
+// flux-divergence stencil is an exact integer sum, rounded once, and one FP64 FMA (the FP64
+// form's other stencils cost eight FP64 operations, or ~20 integer operations a tap).  The S set
+// stays FP64 (the mixed viscous terms as in k_assemble_tma<double>); the centre values of the
+// Laplacians and of the work terms are the FP64 fields, read from global memory.
+struct FxCtx {
+    const int* E;      // exponents of the copy read, field by field
+    const double* Pr;  // the FP64 P set read (centre values)
+    long long c;       // element of cell (T.i0, jc, kc) inside a field
+    long long si, fs;
+    int ni;            // cells of the tile inside the box along i (the rest read the last one)
+    bool xf;           // a sum left FP64's normal range
+};
+__device__ __forceinline__ double fx_centre(const FxCtx& x, int field, int i) {
+    return __ldg(x.Pr + field * x.fs + x.c + (long long)min(i, x.ni - 1) * x.si);
+}
+
+// The full-box (u, v, w or e) pass: FP64 centre weight, then the i, j, k second differences.  The
+// cells of a thread's column are walked by a rolled loop (one copy of the stencil code: eight
+// unrolled copies of 27 fixed-point stencils overflow the instruction cache), taps from shared
+// memory along every axis.
+__device__ __forceinline__ void lap_full_fx(const long long* s, int tj, int tk, double cw, const double* wi,
+                                            const double* wj, const double* wk, double* acc, double* ctr,
+                                            bool init_from_acc, int field, FxCtx& x) {
+    using B = Bx<BX_FULL>;
+    const int E = __ldg(x.E + field);
+#pragma unroll 1
+    for (int i = 0; i < XI; i++) {
+        const double c0 = fx_centre(x, field, i);
+        ctr[i] = c0;
+        double a = init_from_acc ? fma(cw, c0, acc[i]) : cw * c0;
+        const long long* p = s + B::at(i + 4, tj + 4, tk + 4);
+        a = fx_d2acc(a, [&](int m) { return p[m * (B::J * B::K)]; }, E, wi, &x.xf);
+        a = fx_d2acc(a, [&](int m) { return p[m * B::K]; }, E, wj, &x.xf);
+        a = fx_d2acc(a, [&](int m) { return p[m]; }, E, wk, &x.xf);
+        acc[i] = a;
+    }
+}
+
+// A flux field staged in box shape S, differenced along `axis` (0 = i, 1 = j, 2 = k) into acc
+// (first: acc starts at 0).
+template <int S, int AXIS>
+__device__ __forceinline__ void flux_fx(const long long* s, int tj, int tk, int field, const double* a, double* acc,
+                                        bool first, FxCtx& x) {
+    using B = Bx<S>;
+    const int E = __ldg(x.E + field);
+    constexpr int st = AXIS == 0 ? B::J * B::K : (AXIS == 1 ? B::K : 1);
+#pragma unroll 1
+    for (int i = 0; i < XI; i++) {
+        const long long* p = s + B::at(i + B::HI, tj + B::HJ, tk + B::HK);
+        acc[i] = fx_d1acc(first ? 0.0 : acc[i], [&](int m) { return p[m * st]; }, E, a, &x.xf);
+    }
+}
+
+// Field e of a tile's 20 loads (kSched) folded into the sums; P fields as fixed-point words, S
+// fields as FP64 (the same arithmetic as consume_field<double> for those).
+__device__ __forceinline__ void consume_field_fx(int e, const void* buf, const CoefT<double>& cf, int tj, int tk,
+                                                 FxCtx& x, double* dmx, double* dmy, double* dmz, double* de,
+                                                 double* f0, double* c0) {
+    const long long* s = (const long long*)buf;
+    const double* d = (const double*)buf;
+    switch (e) {
+        case 0: {  // SPHI: de starts from eta * Phi
+            using B = Bx<BX_C>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) de[i] = d[B::at(i, tj, tk)];
+            break;
+        }
+        case 1: {  // PT: de = tc e0 + phi, then the x, y, z second differences
+            double t0[XI];
+            lap_full_fx(s, tj, tk, cf.tc, cf.tl[0], cf.tl[1], cf.tl[2], de, t0, true, PT, x);
+            break;
+        }
+        case 2:
+            lap_full_fx(s, tj, tk, cf.vc[0], cf.vl[0][0], cf.vl[0][1], cf.vl[0][2], dmx, c0, false, PU, x);
+            break;
+        case 3: {  // SX: dmx += (eta/3) d/dx (v_y + w_z); then the work term dmx u0
+            using B = Bx<BX_I>;
+            double col[16];
+#pragma unroll
+            for (int ii = 0; ii < 16; ii++) col[ii] = d[B::at(ii, tj, tk)];
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmx[i] = cd1acc<xon(kExactMixed, 0)>(dmx[i], col, i + 4, cf.mx[0]);
+                de[i] = fma(dmx[i], c0[i], de[i]);
+            }
+            break;
+        }
+        case 4:
+            lap_full_fx(s, tj, tk, cf.vc[1], cf.vl[1][0], cf.vl[1][1], cf.vl[1][2], dmy, c0, false, PV, x);
+            break;
+        case 5: {  // SY
+            using B = Bx<BX_J>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmy[i] = sd1acc<xon(kExactMixed, 1)>(dmy[i], d + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
+                de[i] = fma(dmy[i], c0[i], de[i]);
+            }
+            break;
+        }
+        case 6:
+            lap_full_fx(s, tj, tk, cf.vc[2], cf.vl[2][0], cf.vl[2][1], cf.vl[2][2], dmz, c0, false, PW, x);
+            break;
+        case 7: {  // SZ
+            using B = Bx<BX_K>;
+#pragma unroll
+            for (int i = 0; i < XI; i++) {
+                dmz[i] = sd1acc<xon(kExactMixed, 2)>(dmz[i], d + B::at(i, tj, tk + 4), 1, cf.mx[2]);
+                de[i] = fma(dmz[i], c0[i], de[i]);
+            }
+            break;
+        }
+        case 8: flux_fx<BX_I, 0>(s, tj, tk, PMX, cf.ha[0], f0, true, x); break;
+        case 9: flux_fx<BX_J, 1>(s, tj, tk, PMY, cf.ha[1], f0, false, x); break;
+        case 10: flux_fx<BX_K, 2>(s, tj, tk, PMZ, cf.ha[2], f0, false, x); break;
+        case 11: flux_fx<BX_I, 0>(s, tj, tk, PFUU, cf.ha[0], dmx, false, x); break;
+        case 12:  // PFUV: along y -> f1, along x -> f2
+            flux_fx<BX_IJ, 1>(s, tj, tk, PFUV, cf.ha[1], dmx, false, x);
+            flux_fx<BX_IJ, 0>(s, tj, tk, PFUV, cf.ha[0], dmy, false, x);
+            break;
+        case 13:  // PFUW: along z -> f1, along x -> f3
+            flux_fx<BX_IK, 2>(s, tj, tk, PFUW, cf.ha[2], dmx, false, x);
+            flux_fx<BX_IK, 0>(s, tj, tk, PFUW, cf.ha[0], dmz, false, x);
+            break;
+        case 14: flux_fx<BX_J, 1>(s, tj, tk, PFVV, cf.ha[1], dmy, false, x); break;
+        case 15:  // PFVW: along z -> f2, along y -> f3
+            flux_fx<BX_JK, 2>(s, tj, tk, PFVW, cf.ha[2], dmy, false, x);
+            flux_fx<BX_JK, 1>(s, tj, tk, PFVW, cf.ha[1], dmz, false, x);
+            break;
+        case 16: flux_fx<BX_K, 2>(s, tj, tk, PFWW, cf.ha[2], dmz, false, x); break;
+        case 17: flux_fx<BX_I, 0>(s, tj, tk, PHU, cf.ha[0], de, false, x); break;
+        case 18: flux_fx<BX_J, 1>(s, tj, tk, PHV, cf.ha[1], de, false, x); break;
+        default: flux_fx<BX_K, 2>(s, tj, tk, PHW, cf.ha[2], de, false, x); break;
+    }
+}
+
+// A thread's 8 cells on the FP64 fields (a copy that is unusable, or a sum outside FP64's normal
+// range): the direct kernel's arithmetic, parked over the thread's sums in the stash.
+__device__ __noinline__ void assemble_column_fp64(const BoxView& b, const Tile& T, int j, int k, int stage,
+                                                  double* stash, int col) {
+    const int pr = b.sc->pbase ^ ((stage - 1) & 1);
+    const double* Pr = (const double*)b.P[pr];
+    const double* S = (const double*)b.S;
+    for (int i = 0; i < XI; i++) {
+        const int ic = T.i0 + i;
+        if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+        const long long c = cell_off(b, ic, j, k), fs = b.fs;
+        double f[5];
+        assemble_terms_fallback<double>(b, Pr, S, c, __ldg(Pr + PU * fs + c), __ldg(Pr + PV * fs + c),
+                                        __ldg(Pr + PW * fs + c), __ldg(Pr + PT * fs + c), f);
+        for (int l = 0; l < 5; l++) stash[(i * 5 + l) * kTileThreads + col] = f[l];
+    }
+}
+
+// One block per SM (160 KB of shared memory: two 64-bit field buffers), as k_assemble_tma<double>.
+// The write-back also writes the fixed-point copy of the P set it writes; the block's maxima of the
+// written fields go to the box's scalars when the block moves to another box and at its end.
+template <int STAGE>
+__global__ void __launch_bounds__(kTileThreads, 1) k_assemble_fx(const BoxView* __restrict__ boxes,
+                                                              const Tile* __restrict__ tiles, int ntiles) {
+    pdl_enter();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    double* buf[2] = {(double*)smem_raw, (double*)smem_raw + kBufElems};
+    uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(double));
+    __shared__ int s_emax[NPF];
+    const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
+    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    if (my_tiles <= 0) return;
+    const int total = my_tiles * kLoads;
+    if (tid == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (tid < NPF) s_emax[tid] = 0;
+    __syncthreads();
+    constexpr int flip = (STAGE - 1) & 1;
+    if (tid == 0) issue<double, true>(boxes, tiles, blockIdx.x, 0, flip, buf[0], &bar[0]);
+
+    double dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
+    int g = 0, fx_box = -1, fx_set = 0;
+    bool fx_bad = false;
+    for (int it = 0; it < my_tiles; it++) {
+        const int tile = blockIdx.x + it * gridDim.x;
+        const Tile T = tiles[tile];
+        const BoxView& b = boxes[T.box];
+        const int pr = b.sc->pbase ^ flip;
+        if (T.box != fx_box) {
+            fx_flush(boxes, fx_box, fx_set, s_emax, fx_bad);
+            fx_bad = false;
+            fx_box = T.box;
+            fx_set = pr ^ 1;
+        }
+        prefetch_state_l2(b, T, STAGE, tid);
+        const bool usable = !b.sc->fx_bad[pr];
+        const int j = T.j0 + tj, k = T.k0 + tk;
+        FxCtx x{b.sc->fx_e[pr], (const double*)b.P[pr],
+                cell_off(b, T.i0, min(j, b.n[1] - 1), min(k, b.n[2] - 1)), b.si, b.fs, min(XI, b.n[0] - T.i0), false};
+#pragma unroll
+        for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.0;
+        for (int e = 0; e < kLoads; e++, g++) {
+            if (tid == 0 && g + 1 < total) {
+                const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
+                issue<double, true>(boxes, tiles, nt, (g + 1) % kLoads, flip, buf[(g + 1) & 1], &bar[(g + 1) & 1]);
+            }
+            const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(&b.sc->status, HEALTH_TIMEOUT);
+                    mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+                    if (g + 1 < total) mbar_wait_bounded(&bar[(g + 1) & 1], (uint32_t)(((g + 1) >> 1) & 1));
+                }
+                return;
+            }
+            if (usable) consume_field_fx(e, buf[g & 1], b.c64, tj, tk, x, dmx, dmy, dmz, de, f0, c0);
+            __syncthreads();  // buffer g & 1 is free for load g + 2
+        }
+        double* stash = buf[(g - 1) & 1];
+        park_sums(stash, tid, f0, dmx, dmy, dmz, de);
+        if (!usable || x.xf) assemble_column_fp64(b, T, j, k, STAGE, stash, tid);
+        FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false};
+        write_back_plain<STAGE>(b, T, stash, tid, tj, tk, &sink);
+        fx_bad |= sink.bad;
+        __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
+    }
+    fx_flush(boxes, fx_box, fx_set, s_emax, fx_bad);
 }
 
 // ---- warp-specialised variant ------------------------------------------------------------
@@ -979,6 +1211,18 @@ cudaError_t tma_encode_maps(const BoxView& v, void* out) {
     const int sshape[4] = {BX_I, BX_J, BX_K, BX_C};
     for (int q = 0; q < 4; q++)
         if (!one(&m->s[q], v.S, NSF, sshape[q])) return cudaErrorInvalidValue;
+    // the fixed-point copies: the P sets' geometry, 64-bit integer words
+    for (int set = 0; set < 2 && fp64 && v.X[0]; set++)
+        for (int sh = 0; sh < 7; sh++) {
+            const cuuint64_t dims[4] = {g2, g1, g0, (cuuint64_t)NPF};
+            const cuuint64_t strides[3] = {(cuuint64_t)v.sj * 8, (cuuint64_t)v.si * 8, (cuuint64_t)v.fs * 8};
+            const cuuint32_t box[4] = {(cuuint32_t)box_k(sh), (cuuint32_t)box_j(sh), (cuuint32_t)box_i(sh), 1};
+            const cuuint32_t es[4] = {1, 1, 1, 1};
+            if (enc(&m->x[set][sh], CU_TENSOR_MAP_DATA_TYPE_INT64, 4, v.X[set], dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return cudaErrorInvalidValue;
+        }
     return cudaSuccess;
 }
 
@@ -1010,6 +1254,29 @@ cudaError_t launch_assemble_tma64(const BoxView* boxes, const Tile* tiles, int n
     if (stage == 1) return launch_tma_stage<double, 1>(boxes, tiles, ntiles, st);
     if (stage == 2) return launch_tma_stage<double, 2>(boxes, tiles, ntiles, st);
     return launch_tma_stage<double, 3>(boxes, tiles, ntiles, st);
+}
+
+template <int STAGE>
+static cudaError_t launch_fx_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
+    auto fn = k_assemble_fx<STAGE>;
+    constexpr size_t smem = 2 * kBufElems * sizeof(double) + 2 * sizeof(uint64_t);
+    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kTileThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    const int grid = ntiles < nsm * per ? ntiles : nsm * per;
+    return launch_pdl(fn, grid, kTileThreads, smem, st, boxes, tiles, ntiles);
+}
+
+cudaError_t launch_assemble_fx(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (stage == 1) return launch_fx_stage<1>(boxes, tiles, ntiles, st);
+    if (stage == 2) return launch_fx_stage<2>(boxes, tiles, ntiles, st);
+    return launch_fx_stage<3>(boxes, tiles, ntiles, st);
 }
 
 template <class Fn>

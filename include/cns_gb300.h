@@ -256,7 +256,7 @@ int cns_box_set_tile(cns_box *box, const int tlog[3]);
  * All give identical bits.  A new mixed box starts on a TMA kernel when the driver provides the
  * tensor-map encoder; a new FP64 box on the direct kernel, which is the faster one for FP64 on
  * GB300 (the FP64 pipe, not the loads, sets its time). */
-enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2 };
+enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2, CNS_ASSEMBLE_TMA_FX = 3 };
 int cns_box_get_kernel(const cns_box *box, int *kernel);
 int cns_box_set_kernel(cns_box *box, int kernel);
 /* Time trial_steps RK3 steps of the box on every candidate shape (the 12 rectangular ones and
