@@ -373,7 +373,7 @@ def time_box(C, n, prec, warmup, steps, sampler=None):
     from cns_nospec_gb300 import initdata as I
     box = C.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM, precision=prec)
     box.init_field((1.0, 1.0, 1.0), 1e-3, 1)
-    tile, kern, _ = box.autotune(trial_steps=2)
+    tile, kern, _ = box.autotune(trial_steps=4)
     box.advance(warmup)
     box.sync()
     if sampler is not None:
@@ -451,7 +451,9 @@ def fp64_roofline(kernel_ms, klaunch, names, cells, fp64_peak):
                     "counters": "fp64_counters.json: " + name})
     else:
         out.update({"achieved": None, "frac": None, "counters": None})
-    tr = cnt.get("dram_bytes_per_cell")
+    # DRAM bytes per cell measured on a box of this size where there is one (the stencils' plane
+    # re-reads stay in L2 at 128^3, not at 256^3), else the 128^3 figure
+    tr = cnt.get("dram_bytes_per_cell_by_n", {}).get(str(round(cells ** (1 / 3))), cnt.get("dram_bytes_per_cell"))
     out["traffic"] = tr * cells if tr is not None else None
     return out
 

@@ -97,7 +97,6 @@ struct Geometry {
     long long sj, si, fs;
     size_t off_sc, off_dtlog, off_U, off_Us, off_P0, off_P1, off_S, off_view, off_tiles, off_aos, total;
     size_t off_xtiles, off_maps;  // mixed boxes: TMA-assembly tiles and tensor maps
-    size_t off_X0, off_X1;        // plain FP64 boxes: fixed-point copies of the P sets (else 0)
     int ntiles;                   // capacity of the tile list (largest candidate shape)
     int nxtiles;                  // TMA-assembly tiles (8 x 8 x 32 cells)
 };
@@ -174,11 +173,6 @@ static Geometry geometry(const cns_box_desc* d) {
     g.off_P0 = o;      o = align256(o + esz * NPF * g.fs);
     g.off_P1 = o;      o = align256(o + esz * NPF * g.fs);
     g.off_S = o;       o = align256(o + esz * NSF * g.fs);
-    g.off_X0 = g.off_X1 = 0;
-    if (d->precision == CNS_FP64) {
-        g.off_X0 = o;  o = align256(o + sizeof(long long) * NPF * g.fs);
-        g.off_X1 = o;  o = align256(o + sizeof(long long) * NPF * g.fs);
-    }
     g.off_view = o;    o = align256(o + sizeof(BoxView));
     g.off_tiles = o;   o = align256(o + sizeof(Tile) * g.ntiles);
     g.off_aos = o;     o = align256(o + sizeof(double) * CNS_NC * g0 * g1 * g2);
@@ -275,6 +269,8 @@ struct cns_box {
     int nq = 0;
     int queue_tlog[3] = {0, 0, 0};
     int* d_counters = nullptr;   // its plane counts and queue position (n[0] + 1 ints)
+    long long* d_X = nullptr;    // the fixed-point copies of the P sets: allocated when the box first
+                                 // goes onto CNS_ASSEMBLE_TMA_FX (stream-ordered), kept until destroy
 };
 
 extern "C" long long cns_box_bytes(const cns_box_desc* desc) {
@@ -319,10 +315,6 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     v.dtlog = (double*)(b->arena + g.off_dtlog);
     v.cfl = desc->cfl;
     v.precision = desc->precision;
-    if (desc->precision == CNS_FP64) {
-        v.X[0] = (long long*)(b->arena + g.off_X0);
-        v.X[1] = (long long*)(b->arena + g.off_X1);
-    }
     fill_coefs(v, desc);
     b->d_view = (BoxView*)(b->arena + g.off_view);
     b->d_tiles = (Tile*)(b->arena + g.off_tiles);
@@ -389,6 +381,7 @@ extern "C" int cns_box_destroy(cns_box* b) {
         cudaFree(b->d_queue);
         cudaFree(b->d_counters);
     }
+    if (b->d_X) cudaFreeAsync(b->d_X, b->stream);
     cudaFreeAsync(b->arena, b->stream);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);  // released once its queued work is done
     delete b;
@@ -1460,6 +1453,24 @@ static int push_fx(cns_box* b) {
     if (fx == b->view.fx) return CNS_OK;
     CK(cudaStreamSynchronize(b->stream));
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
+    if (fx && !b->d_X) {
+        // the copies (two sets of the P fields' geometry, 64-bit words) and their tensor maps
+        const size_t bytes = sizeof(long long) * 2 * NPF * (size_t)b->view.fs;
+        cudaError_t e = cudaMallocAsync((void**)&b->d_X, bytes, b->stream);
+        if (e != cudaSuccess) {
+            b->d_X = nullptr;
+            cudaGetLastError();
+            return fail(CNS_ERR_NOMEM, "fixed-point copies: %zu bytes of device memory not available", bytes);
+        }
+        b->view.X[0] = b->d_X;
+        b->view.X[1] = b->d_X + NPF * b->view.fs;
+        std::vector<unsigned char> maps(tma_maps_bytes());
+        CK(tma_encode_maps(b->view, maps.data()));
+        CK(cudaMemcpyAsync((void*)b->view.tma, maps.data(), maps.size(), cudaMemcpyHostToDevice, b->stream));
+        CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, X), b->view.X, sizeof b->view.X,
+                           cudaMemcpyHostToDevice, b->stream));
+        CK(cudaStreamSynchronize(b->stream));  // `maps` lives on this stack frame
+    }
     b->view.fx = fx;
     static const int kNone[2] = {0, 0}, kBoth[2] = {1, 1};
     CK(cudaMemcpyAsync(&b->d_sc->fx_bad[0], fx ? kNone : kBoth, sizeof kBoth, cudaMemcpyHostToDevice, b->stream));

@@ -42,28 +42,29 @@ __device__ __forceinline__ const CoefT<double>& coefs<double>(const BoxView& b) 
 template <>
 __device__ __forceinline__ const CoefT<float>& coefs<float>(const BoxView& b) { return b.c32; }
 
-// acc + sum_m a_m (p[m s] - p[-m s]); in the plain form (R = double) the exact sum (cns_exact.cuh)
-// where X.  NB (no branch): the exact sum without its FP64 fallback, *xf set where the fallback
-// is needed (the caller then evaluates the cell again with NB = false; cns_exact.cuh).
-template <bool X, class R, bool NB = false>
-__device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, const R* a, bool* xf = nullptr) {
-    if constexpr (sizeof(R) == 8 && X) {
-        if constexpr (NB) return xd1acc_nb(acc, XTaps<0>{p, s}, a, xf);
-        else return xd1acc(acc, XTaps<0>{p, s}, a);
-    }
-    acc = fma(a[0], __ldg(p + s) - __ldg(p - s), acc);
-    acc = fma(a[1], __ldg(p + 2 * s) - __ldg(p - 2 * s), acc);
-    acc = fma(a[2], __ldg(p + 3 * s) - __ldg(p - 3 * s), acc);
-    acc = fma(a[3], __ldg(p + 4 * s) - __ldg(p - 4 * s), acc);
-    return acc;
-}
 // Loads of stencil taps: through the read-only path (NC, for data no thread of the launch
 // writes), or from L2 past L1 (for data other blocks of the same launch write: L1 is not kept
-// coherent, and a 128-byte line can hold bytes of a row that is not written yet).
+// coherent, and a 128-byte line can hold bytes of a row that is not written yet; and for the S
+// set in the assembly, whose taps reach L1 to no use: the L2 path measured 1 % faster there).
 template <bool NC, class R>
 __device__ __forceinline__ R ld_tap(const R* p) {
     if (NC) return __ldg(p);
     return __ldcg(p);
+}
+// acc + sum_m a_m (p[m s] - p[-m s]); in the plain form (R = double) the exact sum (cns_exact.cuh)
+// where X.  NB (no branch): the exact sum without its FP64 fallback, *xf set where the fallback
+// is needed (the caller then evaluates the cell again with NB = false; cns_exact.cuh).
+template <bool X, class R, bool NB = false, bool NC = true>
+__device__ __forceinline__ R d1acc(R acc, const R* __restrict__ p, long long s, const R* a, bool* xf = nullptr) {
+    if constexpr (sizeof(R) == 8 && X) {
+        if constexpr (NB) return xd1acc_nb(acc, XTaps<NC ? 0 : 1>{p, s}, a, xf);
+        else return xd1acc(acc, XTaps<NC ? 0 : 1>{p, s}, a);
+    }
+    acc = fma(a[0], ld_tap<NC>(p + s) - ld_tap<NC>(p - s), acc);
+    acc = fma(a[1], ld_tap<NC>(p + 2 * s) - ld_tap<NC>(p - 2 * s), acc);
+    acc = fma(a[2], ld_tap<NC>(p + 3 * s) - ld_tap<NC>(p - 3 * s), acc);
+    acc = fma(a[3], ld_tap<NC>(p + 4 * s) - ld_tap<NC>(p - 4 * s), acc);
+    return acc;
 }
 template <bool X, class R, bool NC = true, bool NB = false>
 __device__ __forceinline__ R d1(const R* __restrict__ p, long long s, const R* a, bool* xf = nullptr) {
@@ -243,19 +244,19 @@ __device__ __forceinline__ void assemble_terms(const BoxView& b, const R* __rest
     dmx = d2acc<xon(kExactLap, 0), R, NB>(dmx, pu, si, cf.vl[0][0], xf);
     dmx = d2acc<xon(kExactLap, 1), R, NB>(dmx, pu, sj, cf.vl[0][1], xf);
     dmx = d2acc<xon(kExactLap, 2), R, NB>(dmx, pu, 1, cf.vl[0][2], xf);
-    dmx = d1acc<xon(kExactMixed, 0), R, NB>(dmx, S + SX * fs + c, si, cf.mx[0], xf);
+    dmx = d1acc<xon(kExactMixed, 0), R, NB, false>(dmx, S + SX * fs + c, si, cf.mx[0], xf);
     R dmy = cf.vc[1] * v0;
     dmy = d2acc<xon(kExactLap, 0), R, NB>(dmy, pv, si, cf.vl[1][0], xf);
     dmy = d2acc<xon(kExactLap, 1), R, NB>(dmy, pv, sj, cf.vl[1][1], xf);
     dmy = d2acc<xon(kExactLap, 2), R, NB>(dmy, pv, 1, cf.vl[1][2], xf);
-    dmy = d1acc<xon(kExactMixed, 1), R, NB>(dmy, S + SY * fs + c, sj, cf.mx[1], xf);
+    dmy = d1acc<xon(kExactMixed, 1), R, NB, false>(dmy, S + SY * fs + c, sj, cf.mx[1], xf);
     R dmz = cf.vc[2] * w0;
     dmz = d2acc<xon(kExactLap, 0), R, NB>(dmz, pw, si, cf.vl[2][0], xf);
     dmz = d2acc<xon(kExactLap, 1), R, NB>(dmz, pw, sj, cf.vl[2][1], xf);
     dmz = d2acc<xon(kExactLap, 2), R, NB>(dmz, pw, 1, cf.vl[2][2], xf);
-    dmz = d1acc<xon(kExactMixed, 2), R, NB>(dmz, S + SZ * fs + c, 1, cf.mx[2], xf);
+    dmz = d1acc<xon(kExactMixed, 2), R, NB, false>(dmz, S + SZ * fs + c, 1, cf.mx[2], xf);
     // diffterm energy component (cpu/diffterm.cpp:272-311)
-    R de = fma(cf.tc, t0, __ldg(S + SPHI * fs + c));
+    R de = fma(cf.tc, t0, __ldcg(S + SPHI * fs + c));
     de = d2acc<xon(kExactLap, 0), R, NB>(de, pt, si, cf.tl[0], xf);
     de = d2acc<xon(kExactLap, 1), R, NB>(de, pt, sj, cf.tl[1], xf);
     de = d2acc<xon(kExactLap, 2), R, NB>(de, pt, 1, cf.tl[2], xf);

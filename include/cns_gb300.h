@@ -250,12 +250,17 @@ int cns_box_get_tile(const cns_box *box, int tlog[3]);
 int cns_box_set_tile(cns_box *box, const int tlog[3]);
 /* Assembly kernel of a box: CNS_ASSEMBLE_DIRECT (one cell per thread, stencil taps loaded
  * through L1), CNS_ASSEMBLE_TMA (8x8x32-cell tiles whose 20 stencil fields are staged in shared
- * memory by TMA tensor copies; for FP64 boxes with FP64 tensor maps and one block per SM) or
+ * memory by TMA tensor copies; for FP64 boxes with FP64 tensor maps and one block per SM),
  * CNS_ASSEMBLE_TMA_WS (mixed boxes only: the TMA kernel with one 512-thread block per SM split
- * into a stencil warp group and an FP64 write-back warp group working on consecutive tiles).
- * All give identical bits.  A new mixed box starts on a TMA kernel when the driver provides the
- * tensor-map encoder; a new FP64 box on the direct kernel, which is the faster one for FP64 on
- * GB300 (the FP64 pipe, not the loads, sets its time). */
+ * into a stencil warp group and an FP64 write-back warp group working on consecutive tiles) or
+ * CNS_ASSEMBLE_TMA_FX (FP64 boxes only: the TMA tiles with the stencil fields staged as 62-bit
+ * fixed-point copies that the box keeps beside its FP64 fields, one exponent per field set from
+ * the fields' largest magnitudes; each Laplacian and flux-divergence stencil an exact integer sum
+ * rounded once and one FP64 operation; within ~2e-15 of the direct kernel, not bit-identical).
+ * DIRECT, TMA and TMA_WS give identical bits.  A new mixed box starts on a TMA kernel when the
+ * driver provides the tensor-map encoder; a new FP64 box on the direct kernel, which is the
+ * faster one for FP64 on GB300 (the FP64 pipe, not the loads, sets its time).  The autotuner
+ * keeps an FP64 box's kernel. */
 enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2, CNS_ASSEMBLE_TMA_FX = 3 };
 int cns_box_get_kernel(const cns_box *box, int *kernel);
 int cns_box_set_kernel(cns_box *box, int kernel);
