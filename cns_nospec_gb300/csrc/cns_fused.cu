@@ -43,8 +43,11 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __rest
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
-        // the assembly after this kernel writes the other P set (and its fixed-point copy)
-        if (sizeof(R) == 8) fx_prepare(b, b.sc->pbase ^ ((stage - 1) & 1) ^ 1);
+        // a box on the fixed-point assembly: the assembly after this kernel writes the other P set's
+        // copy; prepared once per box, by the block holding the box's first tile (a store from every
+        // tile, all to the same few words, measured 5 % of this kernel's time)
+        if (sizeof(R) == 8 && b.fx && (t == 0 || tiles[t - 1].box != T.box))
+            fx_prepare(b, b.sc->pbase ^ ((stage - 1) & 1) ^ 1);
         int i, j, k;
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
         if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
@@ -181,15 +184,18 @@ __global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int fli
     }
     s->dt = boxes[bx].cfl / courno;
     s->courno_bits = 0ull;
-    // The plain form's fixed-point exponents: the next step's writes take them from the maxima of
-    // this step's writes (after an upload, of the uploaded P set; after a restore, the restored ones)
-    if (flip || !s->fx_restore) {
-        for (int f = 0; f < NPF; f++) s->fx_prev[f] = s->fx_cur[f];
+    // A box on the fixed-point assembly: the next step's writes take their exponents from the
+    // maxima of this step's writes (after an upload, of the uploaded P set; after a restore, the
+    // restored ones)
+    if (boxes[bx].fx) {
+        if (flip || !s->fx_restore) {
+            for (int f = 0; f < NPF; f++) s->fx_prev[f] = s->fx_cur[f];
+        }
+        for (int f = 0; f < NPF; f++) s->fx_cur[f] = 0;
+        fx_prepare_one(boxes[bx], s->pbase ^ 1);  // written by the next stage 1 (whose derivative
+                                                  // pass may ride with an upload)
     }
-    for (int f = 0; f < NPF; f++) s->fx_cur[f] = 0;
     s->fx_restore = 0;
-    fx_prepare_one(boxes[bx], s->pbase ^ 1);  // written by the next stage 1 (whose derivative pass
-                                              // may ride with an upload)
 }
 
 // ---- k_fx_pass: the fixed-point copy of a box's uploaded P set ------------------------------

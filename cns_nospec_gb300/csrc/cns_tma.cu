@@ -686,6 +686,7 @@ struct FxCtx {
     long long si, fs;
     int ni;            // cells of the tile inside the box along i (the rest read the last one)
     bool xf;           // a sum left FP64's normal range
+    int i0, i1;        // the thread's cells of its column: [i0, i1)
 };
 __device__ __forceinline__ double fx_centre(const FxCtx& x, int field, int i) {
     return __ldg(x.Pr + field * x.fs + x.c + (long long)min(i, x.ni - 1) * x.si);
@@ -701,7 +702,7 @@ __device__ __forceinline__ void lap_full_fx(const long long* s, int tj, int tk, 
     using B = Bx<BX_FULL>;
     const int E = __ldg(x.E + field);
 #pragma unroll 1
-    for (int i = 0; i < XI; i++) {
+    for (int i = x.i0; i < x.i1; i++) {
         const double c0 = fx_centre(x, field, i);
         ctr[i] = c0;
         double a = init_from_acc ? fma(cw, c0, acc[i]) : cw * c0;
@@ -722,7 +723,7 @@ __device__ __forceinline__ void flux_fx(const long long* s, int tj, int tk, int 
     const int E = __ldg(x.E + field);
     constexpr int st = AXIS == 0 ? B::J * B::K : (AXIS == 1 ? B::K : 1);
 #pragma unroll 1
-    for (int i = 0; i < XI; i++) {
+    for (int i = x.i0; i < x.i1; i++) {
         const long long* p = s + B::at(i + B::HI, tj + B::HJ, tk + B::HK);
         acc[i] = fx_d1acc(first ? 0.0 : acc[i], [&](int m) { return p[m * st]; }, E, a, &x.xf);
     }
@@ -738,8 +739,8 @@ __device__ __forceinline__ void consume_field_fx(int e, const void* buf, const C
     switch (e) {
         case 0: {  // SPHI: de starts from eta * Phi
             using B = Bx<BX_C>;
-#pragma unroll
-            for (int i = 0; i < XI; i++) de[i] = d[B::at(i, tj, tk)];
+#pragma unroll 1
+            for (int i = x.i0; i < x.i1; i++) de[i] = d[B::at(i, tj, tk)];
             break;
         }
         case 1: {  // PT: de = tc e0 + phi, then the x, y, z second differences
@@ -752,12 +753,9 @@ __device__ __forceinline__ void consume_field_fx(int e, const void* buf, const C
             break;
         case 3: {  // SX: dmx += (eta/3) d/dx (v_y + w_z); then the work term dmx u0
             using B = Bx<BX_I>;
-            double col[16];
-#pragma unroll
-            for (int ii = 0; ii < 16; ii++) col[ii] = d[B::at(ii, tj, tk)];
-#pragma unroll
-            for (int i = 0; i < XI; i++) {
-                dmx[i] = cd1acc<xon(kExactMixed, 0)>(dmx[i], col, i + 4, cf.mx[0]);
+#pragma unroll 1
+            for (int i = x.i0; i < x.i1; i++) {
+                dmx[i] = sd1acc<xon(kExactMixed, 0)>(dmx[i], d + B::at(i + 4, tj, tk), B::J * B::K, cf.mx[0]);
                 de[i] = fma(dmx[i], c0[i], de[i]);
             }
             break;
@@ -767,8 +765,8 @@ __device__ __forceinline__ void consume_field_fx(int e, const void* buf, const C
             break;
         case 5: {  // SY
             using B = Bx<BX_J>;
-#pragma unroll
-            for (int i = 0; i < XI; i++) {
+#pragma unroll 1
+            for (int i = x.i0; i < x.i1; i++) {
                 dmy[i] = sd1acc<xon(kExactMixed, 1)>(dmy[i], d + B::at(i, tj + 4, tk), B::K, cf.mx[1]);
                 de[i] = fma(dmy[i], c0[i], de[i]);
             }
@@ -779,8 +777,8 @@ __device__ __forceinline__ void consume_field_fx(int e, const void* buf, const C
             break;
         case 7: {  // SZ
             using B = Bx<BX_K>;
-#pragma unroll
-            for (int i = 0; i < XI; i++) {
+#pragma unroll 1
+            for (int i = x.i0; i < x.i1; i++) {
                 dmz[i] = sd1acc<xon(kExactMixed, 2)>(dmz[i], d + B::at(i, tj, tk + 4), 1, cf.mx[2]);
                 de[i] = fma(dmz[i], c0[i], de[i]);
             }
@@ -813,11 +811,11 @@ __device__ __forceinline__ void consume_field_fx(int e, const void* buf, const C
 // A thread's 8 cells on the FP64 fields (a copy that is unusable, or a sum outside FP64's normal
 // range): the direct kernel's arithmetic, parked over the thread's sums in the stash.
 __device__ __noinline__ void assemble_column_fp64(const BoxView& b, const Tile& T, int j, int k, int stage,
-                                                  double* stash, int col) {
+                                                  double* stash, int col, int i0, int i1) {
     const int pr = b.sc->pbase ^ ((stage - 1) & 1);
     const double* Pr = (const double*)b.P[pr];
     const double* S = (const double*)b.S;
-    for (int i = 0; i < XI; i++) {
+    for (int i = i0; i < i1; i++) {
         const int ic = T.i0 + i;
         if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
         const long long c = cell_off(b, ic, j, k), fs = b.fs;
@@ -828,30 +826,108 @@ __device__ __noinline__ void assemble_column_fp64(const BoxView& b, const Tile& 
     }
 }
 
+// write_back_plain for 512-thread blocks: the cells [i0, i1) of column `col`, the stage-3 block
+// maximum over 16 warps.
+template <int STAGE>
+__device__ __forceinline__ void write_back_fx(const BoxView& b, const Tile& T, double* stash, int col, int tj, int tk,
+                                              int i0, int i1, FxSink* fx) {
+    const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
+    double* Pw = (double*)b.P[pr ^ 1];
+    const double dt = b.sc->dt;
+    const int j = T.j0 + tj, k = T.k0 + tk;
+    const long long fs = b.fs;
+    float m32 = -1.0f;
+    int health = 0;
+#pragma unroll 1
+    for (int i = i0; i < i1; i++) {
+        const int ic = T.i0 + i;
+        if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+        const long long c = cell_off(b, ic, j, k);
+        double un[5];
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+            const long long e = c + l * fs;
+            const double r = stash[(i * 5 + l) * kTileThreads + col];
+            if (STAGE == 1) {
+                un[l] = fma(dt, r, b.U[e]);
+                b.Us[e] = un[l];
+            } else if (STAGE == 2) {
+                un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                b.Us[e] = un[l];
+            } else {
+                un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
+                b.U[e] = un[l];
+            }
+        }
+        if (STAGE == 3 && b.host_out) store_host(b, ic, j, k, un);
+        CourantInput64 q;
+        epilogue_plain(b, Pw, c, ic, j, k, un, &health, &q, fx);
+        if (STAGE == 3) {
+            const float est = courant_plain_est(b, q);
+            reinterpret_cast<float*>(stash + (i * 5 + 0) * kTileThreads + col)[0] = est;
+            stash[(i * 5 + 1) * kTileThreads + col] = q.p;
+            m32 = fmaxf(m32, est);
+        }
+    }
+    if (health) atomicOr(&b.sc->status, health);
+    if (STAGE == 3) {
+        constexpr int kW = 2 * kTileThreads / 32;
+        __shared__ float s_max[kW];
+        float m = m32;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+        __syncthreads();
+        m = s_max[0];
+#pragma unroll
+        for (int w = 1; w < kW; w++) m = fmaxf(m, s_max[w]);
+        __syncthreads();
+        const float thr = m * (1.0f - 4.0f * kCourantPlainEps);
+        const float gcut = courant_running_max(b);
+        double cmax = 0.0;
+#pragma unroll 1
+        for (int i = i0; i < i1; i++) {
+            const int ic = T.i0 + i;
+            if (ic >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
+            const float est = reinterpret_cast<const float*>(stash + (i * 5 + 0) * kTileThreads + col)[0];
+            if ((m <= 3.0e38f && est < thr && est > 1e-30f) || courant_below(est, gcut)) continue;
+            const long long c = cell_off(b, ic, j, k);
+            const double rho = b.U[c], rinv = rcp_nr(rho);
+            const CourantInput64 q{stash[(i * 5 + 1) * kTileThreads + col], rinv, b.U[c + fs] * rinv,
+                                   b.U[c + 2 * fs] * rinv, b.U[c + 3 * fs] * rinv};
+            const double cour = courant_plain(b, q);
+            cmax = cour > cmax ? cour : cmax;
+        }
+        courant_fold(b, cmax);
+    }
+}
+
 // One block per SM (160 KB of shared memory: two 64-bit field buffers), as k_assemble_tma<double>.
 // The write-back also writes the fixed-point copy of the P set it writes; the block's maxima of the
 // written fields go to the box's scalars when the block moves to another box and at its end.
 template <int STAGE>
-__global__ void __launch_bounds__(kTileThreads, 1) k_assemble_fx(const BoxView* __restrict__ boxes,
+__global__ void __launch_bounds__(2 * kTileThreads, 1) k_assemble_fx(const BoxView* __restrict__ boxes,
                                                               const Tile* __restrict__ tiles, int ntiles) {
     pdl_enter();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     double* buf[2] = {(double*)smem_raw, (double*)smem_raw + kBufElems};
     uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(double));
     __shared__ int s_emax[NPF];
-    const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
+    // two threads per (j, k) column, four cells of it each
+    const int tid = threadIdx.x & (kTileThreads - 1), half = threadIdx.x >> 8, tk = tid & (XK - 1), tj = tid >> 5;
+    const int ci0 = half * (XI / 2), ci1 = ci0 + XI / 2;
     const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     if (my_tiles <= 0) return;
     const int total = my_tiles * kLoads;
-    if (tid == 0) {
+    if (threadIdx.x == 0) {
         mbar_init(&bar[0]);
         mbar_init(&bar[1]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (tid < NPF) s_emax[tid] = 0;
+    if (threadIdx.x < NPF) s_emax[threadIdx.x] = 0;
     __syncthreads();
     constexpr int flip = (STAGE - 1) & 1;
-    if (tid == 0) issue<double, true>(boxes, tiles, blockIdx.x, 0, flip, buf[0], &bar[0]);
+    if (threadIdx.x == 0) issue<double, true>(boxes, tiles, blockIdx.x, 0, flip, buf[0], &bar[0]);
 
     double dmx[XI], dmy[XI], dmz[XI], de[XI], f0[XI], c0[XI];
     int g = 0, fx_box = -1, fx_set = 0;
@@ -867,21 +943,22 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_assemble_fx(const BoxView* 
             fx_box = T.box;
             fx_set = pr ^ 1;
         }
-        prefetch_state_l2(b, T, STAGE, tid);
+        if (half == 0) prefetch_state_l2(b, T, STAGE, tid);
         const bool usable = !b.sc->fx_bad[pr];
         const int j = T.j0 + tj, k = T.k0 + tk;
         FxCtx x{b.sc->fx_e[pr], (const double*)b.P[pr],
-                cell_off(b, T.i0, min(j, b.n[1] - 1), min(k, b.n[2] - 1)), b.si, b.fs, min(XI, b.n[0] - T.i0), false};
+                cell_off(b, T.i0, min(j, b.n[1] - 1), min(k, b.n[2] - 1)), b.si, b.fs, min(XI, b.n[0] - T.i0), false,
+                ci0, ci1};
 #pragma unroll
         for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.0;
         for (int e = 0; e < kLoads; e++, g++) {
-            if (tid == 0 && g + 1 < total) {
+            if (threadIdx.x == 0 && g + 1 < total) {
                 const int nt = blockIdx.x + ((g + 1) / kLoads) * gridDim.x;
                 issue<double, true>(boxes, tiles, nt, (g + 1) % kLoads, flip, buf[(g + 1) & 1], &bar[(g + 1) & 1]);
             }
             const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
             if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
+                if (threadIdx.x == 0) {
                     atomicOr(&b.sc->status, HEALTH_TIMEOUT);
                     mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
                     if (g + 1 < total) mbar_wait_bounded(&bar[(g + 1) & 1], (uint32_t)(((g + 1) >> 1) & 1));
@@ -892,10 +969,17 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_assemble_fx(const BoxView* 
             __syncthreads();  // buffer g & 1 is free for load g + 2
         }
         double* stash = buf[(g - 1) & 1];
-        park_sums(stash, tid, f0, dmx, dmy, dmz, de);
-        if (!usable || x.xf) assemble_column_fp64(b, T, j, k, STAGE, stash, tid);
+#pragma unroll 1
+        for (int i = ci0; i < ci1; i++) {
+            stash[(i * 5 + 0) * kTileThreads + tid] = f0[i];
+            stash[(i * 5 + 1) * kTileThreads + tid] = dmx[i];
+            stash[(i * 5 + 2) * kTileThreads + tid] = dmy[i];
+            stash[(i * 5 + 3) * kTileThreads + tid] = dmz[i];
+            stash[(i * 5 + 4) * kTileThreads + tid] = de[i];
+        }
+        if (!usable || x.xf) assemble_column_fp64(b, T, j, k, STAGE, stash, tid, ci0, ci1);
         FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false};
-        write_back_plain<STAGE>(b, T, stash, tid, tj, tk, &sink);
+        write_back_fx<STAGE>(b, T, stash, tid, tj, tk, ci0, ci1, &sink);
         fx_bad |= sink.bad;
         __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
     }
@@ -1265,11 +1349,11 @@ static cudaError_t launch_fx_stage(const BoxView* boxes, const Tile* tiles, int 
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, kTileThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)fn, 2 * kTileThreads, smem);
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;
     const int grid = ntiles < nsm * per ? ntiles : nsm * per;
-    return launch_pdl(fn, grid, kTileThreads, smem, st, boxes, tiles, ntiles);
+    return launch_pdl(fn, grid, 2 * kTileThreads, smem, st, boxes, tiles, ntiles);
 }
 
 cudaError_t launch_assemble_fx(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
