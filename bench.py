@@ -56,8 +56,9 @@ def parse():
                    help="profiling case: only upload + warmup + steps of one form (for ncu), then exit; "
                         "e2e: warmup + steps calls of cns_new_advance on a page-locked host array "
                         "(e2e_pageable: on a pageable one)")
-    p.add_argument("--kernel", choices=["ws", "tma", "direct", "fx"], default=None,
-                   help="--case: the assembly kernel (default: the library's choice; ws is mixed-only, fx FP64-only)")
+    p.add_argument("--kernel", choices=["ws", "tma", "direct", "fx", "fxd"], default=None,
+                   help="--case: the assembly kernel (default: the library's choice; ws is mixed-only, fx (TMA) and "
+                        "fxd (direct) on fixed-point taps FP64-only)")
     p.add_argument("--workload", choices=["box", "batch", "mixed256", "serve", "cpu"], default="box",
                    help="box: the headline line (default); batch: 256 uneven boxes; "
                         "mixed256: FP64 vs mixed at --size; serve: the request stream; "
@@ -596,7 +597,7 @@ def run_case(args):
     box = C.Box(args.n, I.box_dx(args.n), I.CFL, I.ETA, I.ALAM, precision=prec)
     if args.kernel:
         box.set_kernel({"ws": C.CNS_ASSEMBLE_TMA_WS, "tma": C.CNS_ASSEMBLE_TMA, "direct": C.CNS_ASSEMBLE_DIRECT,
-                        "fx": C.CNS_ASSEMBLE_TMA_FX}[args.kernel])
+                        "fx": C.CNS_ASSEMBLE_TMA_FX, "fxd": C.CNS_ASSEMBLE_FX}[args.kernel])
     box.init_field(perturb=1e-3, seed=1)
     box.advance_timed(args.warmup)
     ms, launches, total = box.advance_timed(args.steps)

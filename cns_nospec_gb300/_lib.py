@@ -17,7 +17,7 @@ _VP = C.c_void_p
 CNS_OK, CNS_ERR_INVALID, CNS_ERR_NOMEM, CNS_ERR_NONFINITE, CNS_ERR_CUDA, CNS_ERR_CAPACITY, CNS_ERR_NODEVICE = range(7)
 CNS_FP64, CNS_MIXED = 0, 1
 CNS_HEALTH_NONPOS_RHO, CNS_HEALTH_NONFINITE, CNS_HEALTH_NONPOS_EINT, CNS_HEALTH_TIMEOUT = 1, 2, 4, 8
-CNS_ASSEMBLE_DIRECT, CNS_ASSEMBLE_TMA, CNS_ASSEMBLE_TMA_WS, CNS_ASSEMBLE_TMA_FX = 0, 1, 2, 3
+CNS_ASSEMBLE_DIRECT, CNS_ASSEMBLE_TMA, CNS_ASSEMBLE_TMA_WS, CNS_ASSEMBLE_TMA_FX, CNS_ASSEMBLE_FX = 0, 1, 2, 3, 4
 KERN_DERIV, KERN_ASSEMBLE, KERN_STEPEND, KERN_PRIM, KERN_COUNT = range(5)
 KERNEL_NAMES = ("k_deriv", "k_assemble", "k_stepend", "k_prim")
 

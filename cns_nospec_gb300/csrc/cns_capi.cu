@@ -270,7 +270,8 @@ struct cns_box {
     int queue_tlog[3] = {0, 0, 0};
     int* d_counters = nullptr;   // its plane counts and queue position (n[0] + 1 ints)
     long long* d_X = nullptr;    // the fixed-point copies of the P sets: allocated when the box first
-                                 // goes onto CNS_ASSEMBLE_TMA_FX (stream-ordered), kept until destroy
+                                 // goes onto a fixed-point kernel (stream-ordered), kept until destroy
+    int fx_kernel = -1;          // the fixed-point kernel the copies are kept for (-1: none)
 };
 
 extern "C" long long cns_box_bytes(const cns_box_desc* desc) {
@@ -397,8 +398,8 @@ extern "C" int cns_box_set_stream(cns_box* b, void* stream) {
 // Prime a box whose U interior was just written: primitives/fluxes, Courant, first dt.
 // `restore` (a snapshot's scalars) keeps its step count and reference values instead of
 // deriving fresh ones, so a resumed run continues bit for bit.
-// The plain form's fixed-point copy of the P set an upload just wrote (boxes on
-// CNS_ASSEMBLE_TMA_FX): its fields' maxima (unless restored exponents are kept), then the copy.
+// The plain form's fixed-point copy of the P set an upload just wrote (boxes on CNS_ASSEMBLE_FX
+// or CNS_ASSEMBLE_TMA_FX): its fields' maxima (unless restored exponents are kept), then the copy.
 static int fx_after_upload(cns_box* b, bool restored) {
     if (!b->view.fx) return CNS_OK;
     if (!restored) CK(launch_fx_pass(false, b->d_view, b->d_tiles, b->ntiles, b->stream));
@@ -539,6 +540,10 @@ struct WorkLists {
     int ndx32 = 0;
     const Tile* f64 = nullptr;  // FP64 boxes on the fixed-point TMA assembly
     int nf64 = 0;
+    const Tile* dfx64 = nullptr;  // the derivative pass of FP64 boxes that keep fixed-point copies
+    int ndfx64 = 0;
+    const Tile* afx64 = nullptr;  // FP64 boxes on the direct assembly on fixed-point taps
+    int nafx64 = 0;
 };
 
 // One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
@@ -559,11 +564,15 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
     int rc;
     for (int stage = 1; stage <= 3; stage++) {
         if (w.nd64 && !(stage == 1 && skip_first_deriv)) {
-            CK(launch_deriv(0, views, w.d64, w.nd64, stage, st));
+            CK(launch_deriv(kFormPlain, views, w.d64, w.nd64, stage, st));
+            if ((rc = mark(CNS_KERN_DERIV))) return rc;
+        }
+        if (w.ndfx64 && !(stage == 1 && skip_first_deriv)) {
+            CK(launch_deriv(kFormPlainFx, views, w.dfx64, w.ndfx64, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
         if (w.nd32 && !(stage == 1 && skip_first_deriv)) {
-            CK(launch_deriv(1, views, w.d32, w.nd32, stage, st));
+            CK(launch_deriv(kFormMixed, views, w.d32, w.nd32, stage, st));
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
         if (w.ndx32 && !(stage == 1 && skip_first_deriv)) {
@@ -571,7 +580,11 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
             if ((rc = mark(CNS_KERN_DERIV))) return rc;
         }
         if (w.na64) {
-            CK(launch_assemble(0, views, w.a64, w.na64, stage, st));
+            CK(launch_assemble(kFormPlain, views, w.a64, w.na64, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
+        if (w.nafx64) {
+            CK(launch_assemble(kFormPlainFx, views, w.afx64, w.nafx64, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
         if (w.nx64) {
@@ -583,7 +596,7 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
         if (w.na32) {
-            CK(launch_assemble(1, views, w.a32, w.na32, stage, st));
+            CK(launch_assemble(kFormMixed, views, w.a32, w.na32, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
         if (w.nx32) {
@@ -609,11 +622,16 @@ static WorkLists box_lists(const cns_box* b) {
         else
             w.d32 = w.a32 = b->d_tiles, w.nd32 = w.na32 = b->ntiles;
     } else {
-        w.d64 = b->d_tiles, w.nd64 = b->ntiles;
+        if (b->view.fx)
+            w.dfx64 = b->d_tiles, w.ndfx64 = b->ntiles;
+        else
+            w.d64 = b->d_tiles, w.nd64 = b->ntiles;
         if (b->kernel == CNS_ASSEMBLE_TMA)
             w.x64 = b->d_xtiles, w.nx64 = b->nxtiles;
         else if (b->kernel == CNS_ASSEMBLE_TMA_FX)
             w.f64 = b->d_xtiles, w.nf64 = b->nxtiles;
+        else if (b->kernel == CNS_ASSEMBLE_FX)
+            w.afx64 = b->d_tiles, w.nafx64 = b->ntiles;
         else
             w.a64 = b->d_tiles, w.na64 = b->ntiles;
     }
@@ -850,17 +868,17 @@ extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->member
 static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
-    std::vector<Tile> d64, a64, f64, d32, a32, x32, w32, dx32;  // the lists of WorkLists
+    std::vector<Tile> d64, a64, f64, d32, a32, x32, w32, dx32, dfx64, afx64;  // the lists of WorkLists
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
         if (b->desc.precision != CNS_MIXED) {
-            // FP64 members: the direct assembly, or the fixed-point TMA one
-            append_tiles(b->desc.n, b->view.tlog, (int)m, d64);
+            // FP64 members: the direct assembly, on FP64 or fixed-point taps, or the fixed-point TMA one
+            append_tiles(b->desc.n, b->view.tlog, (int)m, b->view.fx ? dfx64 : d64);
             if (b->kernel == CNS_ASSEMBLE_TMA_FX)
                 append_xtiles(b->desc.n, (int)m, f64);
             else
-                append_tiles(b->desc.n, b->view.tlog, (int)m, a64);
+                append_tiles(b->desc.n, b->view.tlog, (int)m, b->kernel == CNS_ASSEMBLE_FX ? afx64 : a64);
             continue;
         }
         if (b->kernel == CNS_ASSEMBLE_TMA || b->kernel == CNS_ASSEMBLE_TMA_WS) {
@@ -872,8 +890,10 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
         }
     }
     std::vector<Tile> all;
-    all.reserve(d64.size() + a64.size() + f64.size() + d32.size() + a32.size() + x32.size() + w32.size() + dx32.size());
-    for (auto* v : {&d64, &a64, &f64, &d32, &a32, &x32, &w32, &dx32}) all.insert(all.end(), v->begin(), v->end());
+    all.reserve(d64.size() + a64.size() + f64.size() + d32.size() + a32.size() + x32.size() + w32.size() + dx32.size() +
+                dfx64.size() + afx64.size());
+    for (auto* v : {&d64, &a64, &f64, &d32, &a32, &x32, &w32, &dx32, &dfx64, &afx64})
+        all.insert(all.end(), v->begin(), v->end());
     const size_t nt = all.size();
     if (views.size() > bt->cap_views) {
         cudaFree(bt->d_views);
@@ -899,7 +919,9 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     w.a32 = at, w.na32 = (int)a32.size(), at += a32.size();
     w.x32 = at, w.nx32 = (int)x32.size(), at += x32.size();
     w.w32 = at, w.nw32 = (int)w32.size(), at += w32.size();
-    w.dx32 = at, w.ndx32 = (int)dx32.size();
+    w.dx32 = at, w.ndx32 = (int)dx32.size(), at += dx32.size();
+    w.dfx64 = at, w.ndfx64 = (int)dfx64.size(), at += dfx64.size();
+    w.afx64 = at, w.nafx64 = (int)afx64.size();
     bt->nviews = (int)views.size();
     if (bt->gexec) {
         cudaGraphExecDestroy(bt->gexec);
@@ -1444,13 +1466,15 @@ static int restore_state(cns_box* b, const BoxScalars* hs) {
     return prime(b, hs);
 }
 
-// A box on CNS_ASSEMBLE_TMA_FX keeps the fixed-point copy of the P set it reads (view.fx); on
-// any other kernel the copies are neither written nor read.  Switching onto it between steps
-// makes the copy of the current P set at once (maxima, then the copy) and takes those maxima for
-// the next writes.
+// A box on CNS_ASSEMBLE_TMA_FX or CNS_ASSEMBLE_FX keeps the fixed-point copy of the P set it reads
+// (view.fx; every field for the TMA kernel, u, v, w, e for the direct ones); on any other kernel
+// the copies are neither written nor read.  Switching onto one of them between steps (or from one
+// to the other) makes the copy of the current P set at once (maxima, then the copy) and takes
+// those maxima for the next writes.
 static int push_fx(cns_box* b) {
-    const int fx = (b->desc.precision == CNS_FP64 && b->kernel == CNS_ASSEMBLE_TMA_FX) ? 1 : 0;
-    if (fx == b->view.fx) return CNS_OK;
+    const int fx =
+        (b->desc.precision == CNS_FP64 && (b->kernel == CNS_ASSEMBLE_TMA_FX || b->kernel == CNS_ASSEMBLE_FX)) ? 1 : 0;
+    if (fx == b->view.fx && (!fx || b->fx_kernel == b->kernel)) return CNS_OK;
     CK(cudaStreamSynchronize(b->stream));
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
     if (fx && !b->d_X) {
@@ -1465,13 +1489,16 @@ static int push_fx(cns_box* b) {
         b->view.X[0] = b->d_X;
         b->view.X[1] = b->d_X + NPF * b->view.fs;
         std::vector<unsigned char> maps(tma_maps_bytes());
-        CK(tma_encode_maps(b->view, maps.data()));
-        CK(cudaMemcpyAsync((void*)b->view.tma, maps.data(), maps.size(), cudaMemcpyHostToDevice, b->stream));
+        if (b->view.tma) {
+            CK(tma_encode_maps(b->view, maps.data()));
+            CK(cudaMemcpyAsync((void*)b->view.tma, maps.data(), maps.size(), cudaMemcpyHostToDevice, b->stream));
+        }
         CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, X), b->view.X, sizeof b->view.X,
                            cudaMemcpyHostToDevice, b->stream));
         CK(cudaStreamSynchronize(b->stream));  // `maps` lives on this stack frame
     }
     b->view.fx = fx;
+    b->fx_kernel = fx ? b->kernel : -1;
     static const int kNone[2] = {0, 0}, kBoth[2] = {1, 1};
     CK(cudaMemcpyAsync(&b->d_sc->fx_bad[0], fx ? kNone : kBoth, sizeof kBoth, cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, fx), &b->view.fx, sizeof(int), cudaMemcpyHostToDevice,
@@ -1488,11 +1515,13 @@ static int push_fx(cns_box* b) {
 
 static int apply_kernel(cns_box* b, int kernel) {
     if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_TMA && kernel != CNS_ASSEMBLE_TMA_WS &&
-        kernel != CNS_ASSEMBLE_TMA_FX)
+        kernel != CNS_ASSEMBLE_TMA_FX && kernel != CNS_ASSEMBLE_FX)
         return fail(CNS_ERR_INVALID, "unknown kernel %d", kernel);
     if (kernel == CNS_ASSEMBLE_TMA_FX && b->desc.precision != CNS_FP64)
         return fail(CNS_ERR_INVALID, "the fixed-point TMA assembly serves plain FP64 boxes only");
-    if (kernel != CNS_ASSEMBLE_DIRECT && !b->view.tma)
+    if (kernel == CNS_ASSEMBLE_FX && b->desc.precision != CNS_FP64)
+        return fail(CNS_ERR_INVALID, "the fixed-point assembly serves plain FP64 boxes only");
+    if (kernel != CNS_ASSEMBLE_DIRECT && kernel != CNS_ASSEMBLE_FX && !b->view.tma)
         return fail(CNS_ERR_INVALID, "the TMA assemblies need the box's tensor maps");
     if (kernel == CNS_ASSEMBLE_TMA_WS && b->desc.precision != CNS_MIXED)
         return fail(CNS_ERR_INVALID, "the warp-specialised TMA assembly serves mixed-precision boxes only");
@@ -1535,7 +1564,7 @@ extern "C" int cns_box_autotune(cns_box* b, int trial_steps, int tlog_out[3], in
     int best[3] = {b->view.tlog[0], b->view.tlog[1], b->view.tlog[2]}, best_k = b->kernel;
     // FP64 boxes keep their arithmetic: on the fixed-point TMA assembly (8x8x32 tiles, nothing to
     // tune but the derivative pass's shape) only the derivative pass's shapes are tried
-    const bool keep_fx = b->kernel == CNS_ASSEMBLE_TMA_FX;
+    const bool keep_fx = b->kernel == CNS_ASSEMBLE_TMA_FX || b->kernel == CNS_ASSEMBLE_FX;
     double best_t = 1e300;
     for (int c = -1; c < nkern * kNumShapes; c++) {  // c = -1: a warm-up trial, not scored
         const int* t = kShapes[c < 0 ? 0 : c % kNumShapes];

@@ -36,7 +36,8 @@ __global__ void __launch_bounds__(kTileThreads) k_prim(const BoxView* __restrict
 }
 
 // ---- k_deriv: first derivatives of (u,v,w) -> mixed-term sums and viscous dissipation -------
-template <class R>
+// FXT: FP64 boxes that keep a fixed-point copy of the P set (deriv_cell).
+template <class R, bool FXT>
 __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
                                                       int ntiles, int stage) {
     pdl_enter();
@@ -51,24 +52,41 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __rest
         int i, j, k;
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
         if (i >= b.n[0] || j >= b.n[1] || k >= b.n[2]) continue;
-        deriv_cell<R>(b, i, j, k, stage);
+        deriv_cell<R, true, FXT>(b, i, j, k, stage);
     }
 }
 
 // ---- k_assemble: D + F, RK stage combine, fused ctoprim/flux/ghost write-back -------------
-template <class R, int STAGE>
+// FXT: FP64 boxes that keep a fixed-point copy of the P set: the kFxLap / kFxFlux stencils read
+// the copy of the set read (where it is usable), and the write-back also writes the copy of the
+// set written, with the block's maxima of its fields (as k_assemble_fx).
+template <class R, int STAGE, bool FXT>
 __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __restrict__ boxes,
                                                          const Tile* __restrict__ tiles, int ntiles) {
     pdl_enter();
+    __shared__ int s_emax[NPF];
+    int fx_box = -1, fx_set = 0;
+    bool fx_bad = false;
+    if (FXT) {
+        if (threadIdx.x < NPF) s_emax[threadIdx.x] = 0;
+        __syncthreads();
+    }
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
+        if (FXT && T.box != fx_box) {
+            fx_flush(boxes, fx_box, fx_set, s_emax, fx_bad);
+            fx_bad = false;
+            fx_box = T.box;
+            fx_set = (b.sc->pbase ^ ((STAGE - 1) & 1)) ^ 1;
+        }
         int i, j, k;
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
         double cour = 0.0;
         int health = 0;
         // plain form, stage 3: the Courant number through FP32 candidates (below)
         constexpr bool kDefer = sizeof(R) == 8 && STAGE == 3;
+        constexpr bool kPlainFx = sizeof(R) == 8 && FXT;
         CourantInput64 cq;
         float est = -1.0f;
         bool inside = false;
@@ -83,7 +101,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
             // diffterm + hypterm (cpu/diffterm.cpp:155-311, cpu/hypterm.cpp:29-208); the plain form
             // with no branch between its exact sums, again with their fallbacks where one needs it
             R f[5];
-            if constexpr (sizeof(R) == 8) {
+            if constexpr (kPlainFx) {
+                const bool usable = !b.sc->fx_bad[pr];
+                bool xf = !usable;
+                if (usable)
+                    assemble_terms<R, true, kFxLap, kFxFlux>(b, Pr, S, c, u0, v0, w0, t0, f, &xf, b.X[pr],
+                                                             b.sc->fx_e[pr]);
+                if (xf) assemble_terms_fallback<R>(b, Pr, S, c, u0, v0, w0, t0, f);
+            } else if constexpr (sizeof(R) == 8) {
                 bool xf = false;
                 assemble_terms<R, true>(b, Pr, S, c, u0, v0, w0, t0, f, &xf);
                 if (xf) assemble_terms_fallback<R>(b, Pr, S, c, u0, v0, w0, t0, f);
@@ -115,7 +140,15 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
                 }
             }
             if (STAGE == 3 && b.host_out) store_host(b, i, j, k, un);
-            if (kDefer) {
+            if (kPlainFx) {
+                FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false, kFxFields};
+                epilogue_plain(b, (double*)Pw, c, i, j, k, un, &health, &cq, &sink);
+                fx_bad |= sink.bad;
+                if (kDefer) {
+                    est = courant_plain_est(b, cq);
+                    inside = true;
+                }
+            } else if (kDefer) {
                 epilogue_plain(b, (double*)Pw, c, i, j, k, un, &health, &cq);
                 est = courant_plain_est(b, cq);
                 inside = true;
@@ -149,6 +182,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
         }
         if (STAGE == 3) courant_fold(b, cour);
     }
+    if (FXT) fx_flush(boxes, fx_box, fx_set, s_emax, fx_bad);
 }
 
 // ---- k_refs: the mixed form's reference values from interior cell (0,0,0) of U ----------
@@ -260,21 +294,21 @@ static cudaError_t launch_prim_t(const BoxView* boxes, const Tile* tiles, int nt
     fn<<<grid_for((const void*)fn, ntiles), kTileThreads, 0, st>>>(boxes, tiles, ntiles);
     return cudaGetLastError();
 }
-template <class R>
+template <class R, bool FXT>
 static cudaError_t launch_deriv_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
-    auto fn = k_deriv<R>;
+    auto fn = k_deriv<R, FXT>;
     return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles, stage);
 }
-template <class R>
+template <class R, bool FXT>
 static cudaError_t launch_assemble_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (stage == 1) {
-        auto fn = k_assemble<R, 1>;
+        auto fn = k_assemble<R, 1, FXT>;
         return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else if (stage == 2) {
-        auto fn = k_assemble<R, 2>;
+        auto fn = k_assemble<R, 2, FXT>;
         return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else {
-        auto fn = k_assemble<R, 3>;
+        auto fn = k_assemble<R, 3, FXT>;
         return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     }
 }
@@ -283,17 +317,18 @@ cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, 
     if (ntiles <= 0) return cudaSuccess;
     return precision ? launch_prim_t<float>(boxes, tiles, ntiles, st) : launch_prim_t<double>(boxes, tiles, ntiles, st);
 }
-cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
-                         cudaStream_t st) {
+cudaError_t launch_deriv(int form, const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (ntiles <= 0) return cudaSuccess;
-    return precision ? launch_deriv_t<float>(boxes, tiles, ntiles, stage, st)
-                     : launch_deriv_t<double>(boxes, tiles, ntiles, stage, st);
+    if (form == kFormMixed) return launch_deriv_t<float, false>(boxes, tiles, ntiles, stage, st);
+    if (form == kFormPlainFx) return launch_deriv_t<double, true>(boxes, tiles, ntiles, stage, st);
+    return launch_deriv_t<double, false>(boxes, tiles, ntiles, stage, st);
 }
-cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
+cudaError_t launch_assemble(int form, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
                             cudaStream_t st) {
     if (ntiles <= 0) return cudaSuccess;
-    return precision ? launch_assemble_t<float>(boxes, tiles, ntiles, stage, st)
-                     : launch_assemble_t<double>(boxes, tiles, ntiles, stage, st);
+    if (form == kFormMixed) return launch_assemble_t<float, false>(boxes, tiles, ntiles, stage, st);
+    if (form == kFormPlainFx) return launch_assemble_t<double, true>(boxes, tiles, ntiles, stage, st);
+    return launch_assemble_t<double, false>(boxes, tiles, ntiles, stage, st);
 }
 cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st) {
     if (nboxes <= 0) return cudaSuccess;

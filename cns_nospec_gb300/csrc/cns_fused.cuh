@@ -92,6 +92,42 @@ __device__ __forceinline__ R d2acc(R acc, const R* __restrict__ p, long long s, 
     return acc;
 }
 
+// ---- stencils on fixed-point taps (FP64 boxes that keep a fixed-point copy of the P set) -----
+// A tap of the copy costs two wide integer multiply-adds (cns_exact.cuh), against ~20 integer
+// instructions to place an FP64 tap's significand for an exact sum.  The direct kernels keep
+// copies of the first kFxFields fields of the P set (u, v, w, e: the derivative pass's and the
+// Laplacians' taps); per family and axis, the masks choose the stencils they evaluate on the
+// copies.  The others stay the FP64 form's (kExact* above).
+constexpr int kFxFields = 4;
+constexpr int kFxDeriv = 0b111, kFxFlux = 0, kFxLap = 0b111;
+static_assert(kFxFlux == 0 || kFxFields == NPF, "flux stencils on copies need copies of every field");
+static_assert(PU < kFxFields && PV < kFxFields && PW < kFxFields && PT < kFxFields, "u, v, w, e have copies");
+
+// 64-bit words of a field's copy at offsets m * s, through the read-only path.
+struct XWords {
+    const long long* p;
+    long long s;
+    __device__ __forceinline__ long long operator()(int m) const { return __ldg(p + m * s); }
+};
+// d1acc / d1 / d2acc of a field whose taps are p (FP64) or, where FXA, x (its copy, exponent E).
+template <bool FXA, bool XA, class R, bool NB>
+__device__ __forceinline__ R tap_d1acc(R acc, const R* p, const long long* x, int E, long long s, const R* a,
+                                       bool* xf) {
+    if constexpr (FXA) return fx_d1acc(acc, XWords{x, s}, E, a, xf);
+    else return d1acc<XA, R, NB>(acc, p, s, a, xf);
+}
+template <bool FXA, bool XA, class R, bool NB>
+__device__ __forceinline__ R tap_d1(const R* p, const long long* x, int E, long long s, const R* a, bool* xf) {
+    if constexpr (FXA) return fx_d1acc(0.0, XWords{x, s}, E, a, xf);
+    else return d1<XA, R, true, NB>(p, s, a, xf);
+}
+template <bool FXA, bool XA, class R, bool NB>
+__device__ __forceinline__ R tap_d2acc(R acc, const R* p, const long long* x, int E, long long s, const R* b,
+                                       bool* xf) {
+    if constexpr (FXA) return fx_d2acc(acc, XWords{x, s}, E, b, xf);
+    else return d2acc<XA, R, NB>(acc, p, s, b, xf);
+}
+
 // Store a value and its periodic face images along the axes in `mask` (1 = i, 2 = j, 4 = k).
 template <class R>
 __device__ __forceinline__ void store_img(R* __restrict__ f, const BoxView& b, long long c, int i, int j, int k,
@@ -186,6 +222,24 @@ __device__ __forceinline__ void deriv9(const R* pu, const R* pv, const R* pw, lo
     d[7] = d1<X1, R, NC, NB>(pw, sj, cf.da[1], xf);
     d[8] = d1<X2, R, NC, NB>(pw, 1, cf.da[2], xf);
 }
+// deriv9 of the plain form with the kFxDeriv axes on the fixed-point copy xu, xv, xw (exponents
+// E); no branch, *xf set where a sum leaves FP64's normal range.
+__device__ __forceinline__ void deriv9_fx(const double* pu, const double* pv, const double* pw, const long long* xu,
+                                          const long long* xv, const long long* xw, const int* E, long long si,
+                                          long long sj, const CoefT<double>& cf, double (&d)[9], bool* xf) {
+    constexpr bool F0 = xon(kFxDeriv, 0), F1 = xon(kFxDeriv, 1), F2 = xon(kFxDeriv, 2);
+    constexpr bool X0 = xon(kExactDeriv, 0), X1 = xon(kExactDeriv, 1), X2 = xon(kExactDeriv, 2);
+    const int eu = E[PU], ev = E[PV], ew = E[PW];
+    d[0] = tap_d1<F0, X0, double, true>(pu, xu, eu, si, cf.da[0], xf);
+    d[1] = tap_d1<F1, X1, double, true>(pu, xu, eu, sj, cf.da[1], xf);
+    d[2] = tap_d1<F2, X2, double, true>(pu, xu, eu, 1, cf.da[2], xf);
+    d[3] = tap_d1<F0, X0, double, true>(pv, xv, ev, si, cf.da[0], xf);
+    d[4] = tap_d1<F1, X1, double, true>(pv, xv, ev, sj, cf.da[1], xf);
+    d[5] = tap_d1<F2, X2, double, true>(pv, xv, ev, 1, cf.da[2], xf);
+    d[6] = tap_d1<F0, X0, double, true>(pw, xw, ew, si, cf.da[0], xf);
+    d[7] = tap_d1<F1, X1, double, true>(pw, xw, ew, sj, cf.da[1], xf);
+    d[8] = tap_d1<F2, X2, double, true>(pw, xw, ew, 1, cf.da[2], xf);
+}
 
 // deriv9 with the exact sums' fallbacks, out of line (as assemble_terms_fallback).
 template <class R, bool NC>
@@ -202,7 +256,9 @@ __device__ __noinline__ void deriv9_fallback(const R* pu, const R* pv, const R* 
 // evaluates the derivatives with no branch between its exact sums and again with their
 // fallbacks in the rare cell that needs one (the same bits either way).
 // NC = false reads the P set from L2 (ld_tap), for a launch whose other blocks write it.
-template <class R, bool NC = true>
+// FXT: a box that keeps a fixed-point copy of the P set (the kFxDeriv axes read the copy where it
+// is usable; the FP64 evaluation where it is not).
+template <class R, bool NC = true, bool FXT = false>
 __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k, int stage) {
     const int pr = b.sc->pbase ^ ((stage - 1) & 1);
     const R* P = (const R*)b.P[pr];
@@ -213,7 +269,16 @@ __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k
     const R* pv = P + PV * fs + c;
     const R* pw = P + PW * fs + c;
     R d[9];
-    if constexpr (sizeof(R) == 8) {
+    if constexpr (sizeof(R) == 8 && FXT) {
+        const bool usable = !b.sc->fx_bad[pr];
+        bool xf = !usable;
+        if (usable) {
+            const long long* X = b.X[pr];
+            deriv9_fx(pu, pv, pw, X + PU * fs + c, X + PV * fs + c, X + PW * fs + c, b.sc->fx_e[pr], si, sj, cf, d,
+                      &xf);
+        }
+        if (xf) deriv9_fallback<R, NC>(pu, pv, pw, si, sj, cf, d);
+    } else if constexpr (sizeof(R) == 8) {
         bool xf = false;
         deriv9<R, NC, true>(pu, pv, pw, si, sj, cf, d, &xf);
         if (xf) deriv9_fallback<R, NC>(pu, pv, pw, si, sj, cf, d);
@@ -230,55 +295,76 @@ __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k
 
 // diffterm + hypterm of one cell (cpu/diffterm.cpp:155-311, cpu/hypterm.cpp:29-208) from the P set
 // Pr and the S set at element c: f[l] = D[l] + F[l].  NB as in d1.
-template <class R, bool NB>
+// FXL / FXF: masks of the Laplacian / flux-divergence axes read from the fixed-point copy Xr of
+// the P set (exponents XE); 0 without a copy.
+template <class R, bool NB, int FXL = 0, int FXF = 0>
 __device__ __forceinline__ void assemble_terms(const BoxView& b, const R* __restrict__ Pr, const R* __restrict__ S,
-                                               long long c, R u0, R v0, R w0, R t0, R (&f)[5], bool* xf) {
+                                               long long c, R u0, R v0, R w0, R t0, R (&f)[5], bool* xf,
+                                               const long long* Xr = nullptr, const int* XE = nullptr) {
     const long long fs = b.fs, si = b.si, sj = b.sj;
     const CoefT<R>& cf = coefs<R>(b);
     const R* pu = Pr + PU * fs + c;
     const R* pv = Pr + PV * fs + c;
     const R* pw = Pr + PW * fs + c;
     const R* pt = Pr + PT * fs + c;
+    constexpr bool XL = FXL != 0, XF = FXF != 0;
+    // the copy's fields at this cell, and their exponents (unused without a copy)
+    auto xat = [&](int f) -> const long long* { return (XL || XF) ? Xr + f * fs + c : nullptr; };
+    auto xe = [&](int f) -> int { return (XL || XF) ? XE[f] : 0; };
     // diffterm momentum components (cpu/diffterm.cpp:155-269)
     R dmx = cf.vc[0] * u0;
-    dmx = d2acc<xon(kExactLap, 0), R, NB>(dmx, pu, si, cf.vl[0][0], xf);
-    dmx = d2acc<xon(kExactLap, 1), R, NB>(dmx, pu, sj, cf.vl[0][1], xf);
-    dmx = d2acc<xon(kExactLap, 2), R, NB>(dmx, pu, 1, cf.vl[0][2], xf);
+    dmx = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmx, pu, xat(PU), xe(PU), si, cf.vl[0][0], xf);
+    dmx = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmx, pu, xat(PU), xe(PU), sj, cf.vl[0][1], xf);
+    dmx = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmx, pu, xat(PU), xe(PU), 1, cf.vl[0][2], xf);
     dmx = d1acc<xon(kExactMixed, 0), R, NB, false>(dmx, S + SX * fs + c, si, cf.mx[0], xf);
     R dmy = cf.vc[1] * v0;
-    dmy = d2acc<xon(kExactLap, 0), R, NB>(dmy, pv, si, cf.vl[1][0], xf);
-    dmy = d2acc<xon(kExactLap, 1), R, NB>(dmy, pv, sj, cf.vl[1][1], xf);
-    dmy = d2acc<xon(kExactLap, 2), R, NB>(dmy, pv, 1, cf.vl[1][2], xf);
+    dmy = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmy, pv, xat(PV), xe(PV), si, cf.vl[1][0], xf);
+    dmy = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmy, pv, xat(PV), xe(PV), sj, cf.vl[1][1], xf);
+    dmy = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmy, pv, xat(PV), xe(PV), 1, cf.vl[1][2], xf);
     dmy = d1acc<xon(kExactMixed, 1), R, NB, false>(dmy, S + SY * fs + c, sj, cf.mx[1], xf);
     R dmz = cf.vc[2] * w0;
-    dmz = d2acc<xon(kExactLap, 0), R, NB>(dmz, pw, si, cf.vl[2][0], xf);
-    dmz = d2acc<xon(kExactLap, 1), R, NB>(dmz, pw, sj, cf.vl[2][1], xf);
-    dmz = d2acc<xon(kExactLap, 2), R, NB>(dmz, pw, 1, cf.vl[2][2], xf);
+    dmz = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmz, pw, xat(PW), xe(PW), si, cf.vl[2][0], xf);
+    dmz = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmz, pw, xat(PW), xe(PW), sj, cf.vl[2][1], xf);
+    dmz = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmz, pw, xat(PW), xe(PW), 1, cf.vl[2][2], xf);
     dmz = d1acc<xon(kExactMixed, 2), R, NB, false>(dmz, S + SZ * fs + c, 1, cf.mx[2], xf);
     // diffterm energy component (cpu/diffterm.cpp:272-311)
     R de = fma(cf.tc, t0, __ldcg(S + SPHI * fs + c));
-    de = d2acc<xon(kExactLap, 0), R, NB>(de, pt, si, cf.tl[0], xf);
-    de = d2acc<xon(kExactLap, 1), R, NB>(de, pt, sj, cf.tl[1], xf);
-    de = d2acc<xon(kExactLap, 2), R, NB>(de, pt, 1, cf.tl[2], xf);
+    de = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(de, pt, xat(PT), xe(PT), si, cf.tl[0], xf);
+    de = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(de, pt, xat(PT), xe(PT), sj, cf.tl[1], xf);
+    de = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(de, pt, xat(PT), xe(PT), 1, cf.tl[2], xf);
     de = fma(dmx, u0, de);
     de = fma(dmy, v0, de);
     de = fma(dmz, w0, de);
     // hypterm (cpu/hypterm.cpp:29-208), added to D
-    f[0] = d1<xon(kExactFlux, 0), R, true, NB>(Pr + PMX * fs + c, si, cf.ha[0], xf);
-    f[0] = d1acc<xon(kExactFlux, 1), R, NB>(f[0], Pr + PMY * fs + c, sj, cf.ha[1], xf);
-    f[0] = d1acc<xon(kExactFlux, 2), R, NB>(f[0], Pr + PMZ * fs + c, 1, cf.ha[2], xf);
-    f[1] = d1acc<xon(kExactFlux, 0), R, NB>(dmx, Pr + PFUU * fs + c, si, cf.ha[0], xf);
-    f[1] = d1acc<xon(kExactFlux, 1), R, NB>(f[1], Pr + PFUV * fs + c, sj, cf.ha[1], xf);
-    f[1] = d1acc<xon(kExactFlux, 2), R, NB>(f[1], Pr + PFUW * fs + c, 1, cf.ha[2], xf);
-    f[2] = d1acc<xon(kExactFlux, 0), R, NB>(dmy, Pr + PFUV * fs + c, si, cf.ha[0], xf);
-    f[2] = d1acc<xon(kExactFlux, 1), R, NB>(f[2], Pr + PFVV * fs + c, sj, cf.ha[1], xf);
-    f[2] = d1acc<xon(kExactFlux, 2), R, NB>(f[2], Pr + PFVW * fs + c, 1, cf.ha[2], xf);
-    f[3] = d1acc<xon(kExactFlux, 0), R, NB>(dmz, Pr + PFUW * fs + c, si, cf.ha[0], xf);
-    f[3] = d1acc<xon(kExactFlux, 1), R, NB>(f[3], Pr + PFVW * fs + c, sj, cf.ha[1], xf);
-    f[3] = d1acc<xon(kExactFlux, 2), R, NB>(f[3], Pr + PFWW * fs + c, 1, cf.ha[2], xf);
-    f[4] = d1acc<xon(kExactFlux, 0), R, NB>(de, Pr + PHU * fs + c, si, cf.ha[0], xf);
-    f[4] = d1acc<xon(kExactFlux, 1), R, NB>(f[4], Pr + PHV * fs + c, sj, cf.ha[1], xf);
-    f[4] = d1acc<xon(kExactFlux, 2), R, NB>(f[4], Pr + PHW * fs + c, 1, cf.ha[2], xf);
+    f[0] = tap_d1<xon(FXF, 0), xon(kExactFlux, 0), R, NB>(Pr + PMX * fs + c, xat(PMX), xe(PMX), si, cf.ha[0], xf);
+    f[0] = tap_d1acc<xon(FXF, 1), xon(kExactFlux, 1), R, NB>(f[0], Pr + PMY * fs + c, xat(PMY), xe(PMY), sj,
+                                                                  cf.ha[1], xf);
+    f[0] = tap_d1acc<xon(FXF, 2), xon(kExactFlux, 2), R, NB>(f[0], Pr + PMZ * fs + c, xat(PMZ), xe(PMZ), 1,
+                                                                  cf.ha[2], xf);
+    f[1] = tap_d1acc<xon(FXF, 0), xon(kExactFlux, 0), R, NB>(dmx, Pr + PFUU * fs + c, xat(PFUU), xe(PFUU), si,
+                                                                  cf.ha[0], xf);
+    f[1] = tap_d1acc<xon(FXF, 1), xon(kExactFlux, 1), R, NB>(f[1], Pr + PFUV * fs + c, xat(PFUV), xe(PFUV), sj,
+                                                                  cf.ha[1], xf);
+    f[1] = tap_d1acc<xon(FXF, 2), xon(kExactFlux, 2), R, NB>(f[1], Pr + PFUW * fs + c, xat(PFUW), xe(PFUW), 1,
+                                                                  cf.ha[2], xf);
+    f[2] = tap_d1acc<xon(FXF, 0), xon(kExactFlux, 0), R, NB>(dmy, Pr + PFUV * fs + c, xat(PFUV), xe(PFUV), si,
+                                                                  cf.ha[0], xf);
+    f[2] = tap_d1acc<xon(FXF, 1), xon(kExactFlux, 1), R, NB>(f[2], Pr + PFVV * fs + c, xat(PFVV), xe(PFVV), sj,
+                                                                  cf.ha[1], xf);
+    f[2] = tap_d1acc<xon(FXF, 2), xon(kExactFlux, 2), R, NB>(f[2], Pr + PFVW * fs + c, xat(PFVW), xe(PFVW), 1,
+                                                                  cf.ha[2], xf);
+    f[3] = tap_d1acc<xon(FXF, 0), xon(kExactFlux, 0), R, NB>(dmz, Pr + PFUW * fs + c, xat(PFUW), xe(PFUW), si,
+                                                                  cf.ha[0], xf);
+    f[3] = tap_d1acc<xon(FXF, 1), xon(kExactFlux, 1), R, NB>(f[3], Pr + PFVW * fs + c, xat(PFVW), xe(PFVW), sj,
+                                                                  cf.ha[1], xf);
+    f[3] = tap_d1acc<xon(FXF, 2), xon(kExactFlux, 2), R, NB>(f[3], Pr + PFWW * fs + c, xat(PFWW), xe(PFWW), 1,
+                                                                  cf.ha[2], xf);
+    f[4] = tap_d1acc<xon(FXF, 0), xon(kExactFlux, 0), R, NB>(de, Pr + PHU * fs + c, xat(PHU), xe(PHU), si,
+                                                                  cf.ha[0], xf);
+    f[4] = tap_d1acc<xon(FXF, 1), xon(kExactFlux, 1), R, NB>(f[4], Pr + PHV * fs + c, xat(PHV), xe(PHV), sj,
+                                                                  cf.ha[1], xf);
+    f[4] = tap_d1acc<xon(FXF, 2), xon(kExactFlux, 2), R, NB>(f[4], Pr + PHW * fs + c, xat(PHW), xe(PHW), 1,
+                                                                  cf.ha[2], xf);
 }
 
 // assemble_terms with the exact sums' fallbacks, out of line: the rare cell that needs one takes
@@ -318,6 +404,7 @@ struct FxSink {
     const int* E;
     int* s_emax;
     bool bad;
+    int nf;  // fields with a copy: the first nf of the set
 };
 __device__ __forceinline__ void fx_store(FxSink& fx, const BoxView& b, long long c, int i, int j, int k, int f,
                                          double v, int mask) {
@@ -443,7 +530,7 @@ __device__ __forceinline__ void epilogue_plain(const BoxView& b, double* __restr
     // occupancy, and the FP64-bound kernels gain nothing from fewer store instructions.
     auto put = [&](int f, double val, int mask) {
         store_img(Pw + f * fs, b, c, i, j, k, val, mask);
-        if (fx) fx_store(*fx, b, c, i, j, k, f, val, mask);
+        if (fx && f < fx->nf) fx_store(*fx, b, c, i, j, k, f, val, mask);
     };
     put(PU, u, 7);
     put(PV, v, 7);

@@ -27,11 +27,12 @@ cudaError_t launch_pdl(void (*fn)(Params...), dim3 grid, dim3 block, size_t smem
 // record the calling thread's last error (read back by cns_last_error); returns `code`
 int set_error(int code, const char* msg);
 
-// fused RK3 stage kernels (cns_fused.cu); precision 0 = FP64 stencils, 1 = FP32 stencils
+// fused RK3 stage kernels (cns_fused.cu); precision / form 0 = FP64 stencils, 1 = FP32 stencils,
+// 2 = FP64 boxes that keep a fixed-point copy of the P set (part of the stencils on the copy)
+constexpr int kFormPlain = 0, kFormMixed = 1, kFormPlainFx = 2;
 cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st);
-cudaError_t launch_deriv(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
-                         cudaStream_t st);
-cudaError_t launch_assemble(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
+cudaError_t launch_deriv(int form, const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
+cudaError_t launch_assemble(int form, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,
                             cudaStream_t st);
 cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st);
 // the plain form's fixed-point copy of an uploaded P set: its fields' maxima (convert = false),

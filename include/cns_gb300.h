@@ -256,12 +256,16 @@ int cns_box_set_tile(cns_box *box, const int tlog[3]);
  * CNS_ASSEMBLE_TMA_FX (FP64 boxes only: the TMA tiles with the stencil fields staged as 62-bit
  * fixed-point copies that the box keeps beside its FP64 fields, one exponent per field set from
  * the fields' largest magnitudes; each Laplacian and flux-divergence stencil an exact integer sum
- * rounded once and one FP64 operation; within ~2e-15 of the direct kernel, not bit-identical).
+ * rounded once and one FP64 operation; within ~2e-15 of the direct kernel, not bit-identical) or
+ * CNS_ASSEMBLE_FX (FP64 boxes only: the direct kernels, with the stencils that the FP64 form sums
+ * exactly on the integer pipes reading the same fixed-point copies instead of placing each FP64
+ * tap's significand; within ~2e-15 of the direct kernel, not bit-identical).
  * DIRECT, TMA and TMA_WS give identical bits.  A new mixed box starts on a TMA kernel when the
  * driver provides the tensor-map encoder; a new FP64 box on the direct kernel, which is the
  * faster one for FP64 on GB300 (the FP64 pipe, not the loads, sets its time).  The autotuner
  * keeps an FP64 box's kernel. */
-enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2, CNS_ASSEMBLE_TMA_FX = 3 };
+enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2, CNS_ASSEMBLE_TMA_FX = 3,
+       CNS_ASSEMBLE_FX = 4 };
 int cns_box_get_kernel(const cns_box *box, int *kernel);
 int cns_box_set_kernel(cns_box *box, int kernel);
 /* Time trial_steps RK3 steps of the box on every candidate shape (the 12 rectangular ones and
