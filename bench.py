@@ -533,8 +533,11 @@ def run_ours(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(n),
-        "form": {"plain": "FP64; 19 of the 39 8-tap stencil sums per cell and stage formed in 64-bit integers on "
-                          "the significands and rounded once to FP64",
+        "form": {"plain": "FP64 (CNS_ASSEMBLE_FX); of the 39 8-tap stencil sums per cell and stage, the 21 of the "
+                          "derivative pass and the Laplacians are exact integer sums of 62-bit fixed-point copies of "
+                          "u, v, w, e and the 5 k-axis flux divergences exact integer sums of the FP64 significands, "
+                          "each rounded once to FP64; the other 13 FP64 chains",
+                 "plain_kernel": {C.CNS_ASSEMBLE_FX: "fx", C.CNS_ASSEMBLE_DIRECT: "direct"}.get(f64["kernel"], "other"),
                  "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
                  "tile_log2_ijk": {"fp64": list(f64["tile"]), "mixed": list(mix["tile"])},
                  "mixed_assembly_kernel": {C.CNS_ASSEMBLE_TMA: "tma", C.CNS_ASSEMBLE_TMA_WS: "tma_ws"}.get(

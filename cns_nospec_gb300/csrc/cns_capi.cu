@@ -97,6 +97,7 @@ struct Geometry {
     long long sj, si, fs;
     size_t off_sc, off_dtlog, off_U, off_Us, off_P0, off_P1, off_S, off_view, off_tiles, off_aos, total;
     size_t off_xtiles, off_maps;  // mixed boxes: TMA-assembly tiles and tensor maps
+    size_t off_X;                 // FP64 boxes: fixed-point copies of kFxFields fields of both P sets
     int ntiles;                   // capacity of the tile list (largest candidate shape)
     int nxtiles;                  // TMA-assembly tiles (8 x 8 x 32 cells)
 };
@@ -176,6 +177,8 @@ static Geometry geometry(const cns_box_desc* d) {
     g.off_view = o;    o = align256(o + sizeof(BoxView));
     g.off_tiles = o;   o = align256(o + sizeof(Tile) * g.ntiles);
     g.off_aos = o;     o = align256(o + sizeof(double) * CNS_NC * g0 * g1 * g2);
+    g.off_X = o;
+    if (d->precision != CNS_MIXED) o = align256(o + sizeof(long long) * 2 * kFxFields * g.fs);
     int xi, xj, xk;
     tma_tile_shape(&xi, &xj, &xk);
     g.nxtiles = 0;
@@ -269,8 +272,9 @@ struct cns_box {
     int nq = 0;
     int queue_tlog[3] = {0, 0, 0};
     int* d_counters = nullptr;   // its plane counts and queue position (n[0] + 1 ints)
-    long long* d_X = nullptr;    // the fixed-point copies of the P sets: allocated when the box first
-                                 // goes onto a fixed-point kernel (stream-ordered), kept until destroy
+    long long* a_X = nullptr;    // FP64 boxes: copies of kFxFields fields of both P sets (arena)
+    long long* d_X = nullptr;    // copies of all NPF fields of both P sets: allocated when the box first
+                                 // goes onto CNS_ASSEMBLE_TMA_FX (stream-ordered), kept until destroy
     int fx_kernel = -1;          // the fixed-point kernel the copies are kept for (-1: none)
 };
 
@@ -321,6 +325,15 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     b->d_tiles = (Tile*)(b->arena + g.off_tiles);
     b->d_aos = (double*)(b->arena + g.off_aos);
     b->d_sc = v.sc;
+    if (desc->precision != CNS_MIXED) {
+        // FP64 boxes start on the direct kernels on fixed-point copies of u, v, w, e
+        b->a_X = (long long*)(b->arena + g.off_X);
+        v.X[0] = b->a_X;
+        v.X[1] = b->a_X + kFxFields * g.fs;
+        v.fx = kFxFields;
+        b->kernel = CNS_ASSEMBLE_FX;
+        b->fx_kernel = CNS_ASSEMBLE_FX;
+    }
     default_tlog(desc->n, v.tlog);
     std::vector<Tile> tiles;
     append_tiles(desc->n, v.tlog, 0, tiles);
@@ -422,6 +435,7 @@ static int prime(cns_box* b, const BoxScalars* restore = nullptr) {
         // writes take theirs from the saved maxima, so the run continues bit for bit
         fx_restored = b->view.fx && !restore->fx_bad[restore->pbase & 1];
         s.fx_restore = fx_restored ? 1 : 0;
+        s.fx_fresh = fx_restored ? restore->fx_fresh : 0;
         for (int f = 0; f < NPF && fx_restored; f++) {
             s.fx_e[0][f] = restore->fx_e[restore->pbase & 1][f];
             s.fx_prev[f] = restore->fx_prev[f];
@@ -1320,7 +1334,8 @@ struct SnapHeader {
     double p_ref, e_ref, E_ref, H_ref, dt_last;
     int64_t payload_doubles;
     // version 2: the fixed-point exponents of the saved P set and the maxima the next writes take
-    // theirs from (fx_valid = 0: none; they are derived again at load)
+    // theirs from (fx_valid = 0: none, they are derived again at load; 2: as 1, and the copy was
+    // made from an upload, fx_fresh)
     int32_t fx_valid, fx_e[NPF], fx_prev[NPF];
 };
 
@@ -1353,7 +1368,7 @@ extern "C" int cns_box_save(cns_box* b, const char* path) {
     h.H_ref = hs.H_ref;
     h.dt_last = hs.dt_last;
     h.payload_doubles = (int64_t)U.size();
-    h.fx_valid = (b->view.fx && !hs.fx_bad[hs.pbase & 1]) ? 1 : 0;
+    h.fx_valid = (b->view.fx && !hs.fx_bad[hs.pbase & 1]) ? (hs.fx_fresh ? 2 : 1) : 0;
     for (int q = 0; q < NPF; q++) {
         h.fx_e[q] = hs.fx_e[hs.pbase & 1][q];
         h.fx_prev[q] = hs.fx_prev[q];
@@ -1402,6 +1417,7 @@ extern "C" int cns_box_load(cns_box* b, const char* path) {
     s.H_ref = h.H_ref;
     s.pbase = 0;
     s.fx_bad[0] = h.fx_valid ? 0 : 1;
+    s.fx_fresh = h.fx_valid == 2 ? 1 : 0;
     for (int q = 0; q < NPF; q++) {
         s.fx_e[0][q] = h.fx_e[q];
         s.fx_prev[q] = h.fx_prev[q];
@@ -1466,19 +1482,19 @@ static int restore_state(cns_box* b, const BoxScalars* hs) {
     return prime(b, hs);
 }
 
-// A box on CNS_ASSEMBLE_TMA_FX or CNS_ASSEMBLE_FX keeps the fixed-point copy of the P set it reads
-// (view.fx; every field for the TMA kernel, u, v, w, e for the direct ones); on any other kernel
-// the copies are neither written nor read.  Switching onto one of them between steps (or from one
-// to the other) makes the copy of the current P set at once (maxima, then the copy) and takes
-// those maxima for the next writes.
+// A box on CNS_ASSEMBLE_FX or CNS_ASSEMBLE_TMA_FX keeps the fixed-point copy of the P set it reads
+// (view.fx fields: u, v, w, e in the box's arena for the direct kernels; every field in a separate
+// allocation for the TMA kernel); on any other kernel the copies are neither written nor read.
+// Switching onto one of them between steps (or from one to the other) makes the copy of the
+// current P set at once (maxima, then the copy) and takes those maxima for the next writes.
 static int push_fx(cns_box* b) {
-    const int fx =
-        (b->desc.precision == CNS_FP64 && (b->kernel == CNS_ASSEMBLE_TMA_FX || b->kernel == CNS_ASSEMBLE_FX)) ? 1 : 0;
+    const bool fp64 = b->desc.precision == CNS_FP64;
+    const int fx = !fp64 ? 0 : b->kernel == CNS_ASSEMBLE_TMA_FX ? NPF : b->kernel == CNS_ASSEMBLE_FX ? kFxFields : 0;
     if (fx == b->view.fx && (!fx || b->fx_kernel == b->kernel)) return CNS_OK;
     CK(cudaStreamSynchronize(b->stream));
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
-    if (fx && !b->d_X) {
-        // the copies (two sets of the P fields' geometry, 64-bit words) and their tensor maps
+    if (fx == NPF && !b->d_X) {
+        // copies of every field (two sets of the P fields' geometry, 64-bit words)
         const size_t bytes = sizeof(long long) * 2 * NPF * (size_t)b->view.fs;
         cudaError_t e = cudaMallocAsync((void**)&b->d_X, bytes, b->stream);
         if (e != cudaSuccess) {
@@ -1486,19 +1502,19 @@ static int push_fx(cns_box* b) {
             cudaGetLastError();
             return fail(CNS_ERR_NOMEM, "fixed-point copies: %zu bytes of device memory not available", bytes);
         }
-        b->view.X[0] = b->d_X;
-        b->view.X[1] = b->d_X + NPF * b->view.fs;
-        std::vector<unsigned char> maps(tma_maps_bytes());
-        if (b->view.tma) {
-            CK(tma_encode_maps(b->view, maps.data()));
-            CK(cudaMemcpyAsync((void*)b->view.tma, maps.data(), maps.size(), cudaMemcpyHostToDevice, b->stream));
-        }
-        CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, X), b->view.X, sizeof b->view.X,
-                           cudaMemcpyHostToDevice, b->stream));
-        CK(cudaStreamSynchronize(b->stream));  // `maps` lives on this stack frame
     }
+    long long* base = fx == NPF ? b->d_X : b->a_X;
+    b->view.X[0] = fx ? base : nullptr;
+    b->view.X[1] = fx ? base + (long long)fx * b->view.fs : nullptr;
     b->view.fx = fx;
     b->fx_kernel = fx ? b->kernel : -1;
+    std::vector<unsigned char> maps(tma_maps_bytes());
+    if (b->view.tma) {  // the TMA kernels' tensor maps, with the copies' when every field has one
+        CK(tma_encode_maps(b->view, maps.data()));
+        CK(cudaMemcpyAsync((void*)b->view.tma, maps.data(), maps.size(), cudaMemcpyHostToDevice, b->stream));
+    }
+    CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, X), b->view.X, sizeof b->view.X, cudaMemcpyHostToDevice,
+                       b->stream));
     static const int kNone[2] = {0, 0}, kBoth[2] = {1, 1};
     CK(cudaMemcpyAsync(&b->d_sc->fx_bad[0], fx ? kNone : kBoth, sizeof kBoth, cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemcpyAsync((char*)b->d_view + offsetof(BoxView, fx), &b->view.fx, sizeof(int), cudaMemcpyHostToDevice,
@@ -1508,7 +1524,7 @@ static int push_fx(cns_box* b) {
         if (rc) return rc;
         CK(launch_fx_adopt(b->d_view, 1, b->stream));
     }
-    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaStreamSynchronize(b->stream));  // `maps` lives on this stack frame
     if (b->batch) b->batch->dirty = true;
     return CNS_OK;
 }

@@ -86,9 +86,12 @@ struct BoxScalars {
     // exponent of field f in it; fx_prev[f] / fx_cur[f] the largest biased exponent field of P
     // field f over the previous step's writes / the writes since.  fx_restore: the box was just
     // restored with its exponents (the conversion after the upload keeps fx_e, and fx_prev stays).
+    // fx_fresh: the copy was made from an upload (not written by a step) and the step after it
+    // has not ended; that step's first derivative pass reads the FP64 fields, as the upload fused
+    // with that pass (host arrays read in place) does, so both routes give the same bits.
     int fx_bad[2];
     int fx_restore;
-    int fx_pad;
+    int fx_fresh;
     int fx_e[2][NPF];
     int fx_prev[NPF];
     int fx_cur[NPF];
@@ -121,10 +124,14 @@ struct BoxView {
                             // (256 threads, one cell each, k fastest across a warp)
     CoefT<double> c64;
     CoefT<float> c32;
-    long long* X[2];        // plain FP64 boxes: fixed-point copies of P[0], P[1] (NPF fields each,
-                            // the P sets' geometry); null for mixed boxes
-    int fx;                 // the box's assembly reads the fixed-point copies (CNS_ASSEMBLE_TMA_FX)
+    long long* X[2];        // plain FP64 boxes: fixed-point copies of the first `fx` fields of P[0],
+                            // P[1] (the P sets' geometry, fields fs apart)
+    int fx;                 // fields with copies: 0 (none), kFxFields (CNS_ASSEMBLE_FX) or NPF
+                            // (CNS_ASSEMBLE_TMA_FX)
 };
+// The fields the direct kernels keep fixed-point copies of: u, v, w, e (the derivative pass's and
+// the Laplacians' taps; PU..PT).
+constexpr int kFxFields = 4;
 
 // A unit of work: one tile of one box, with origin (i0, j0, k0); its shape is the box's tlog.
 struct Tile {

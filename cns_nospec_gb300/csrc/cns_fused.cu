@@ -215,6 +215,7 @@ __global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int fli
         s->dt_last = s->dt;
         s->pbase ^= 1;
         s->nsteps_done += 1;
+        s->fx_fresh = 0;
     }
     s->dt = boxes[bx].cfl / courno;
     s->courno_bits = 0ull;
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(kTileThreads) k_fx_pass(const BoxView* __restr
             fx_set = W;
             if (CONVERT && !sc->fx_restore && threadIdx.x < NPF)
                 sc->fx_e[W][threadIdx.x] = fx_exponent(sc->fx_cur[threadIdx.x]);
+            if (CONVERT && !sc->fx_restore && threadIdx.x == 0) sc->fx_fresh = 1;
         }
         int i, j, k;
         tile_pos(b, T, threadIdx.x, &i, &j, &k);
@@ -263,6 +265,7 @@ __global__ void __launch_bounds__(kTileThreads) k_fx_pass(const BoxView* __restr
             const long long c = cell_off(b, i, j, k);
 #pragma unroll
             for (int f = 0; f < NPF; f++) {
+                if (f >= b.fx) break;  // fields without a copy
                 const double v = P[f * b.fs + c];
                 if (!CONVERT) {
                     fx_track(s_emax + f, fx_efield(v));

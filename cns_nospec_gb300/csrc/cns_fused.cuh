@@ -97,8 +97,9 @@ __device__ __forceinline__ R d2acc(R acc, const R* __restrict__ p, long long s, 
 // instructions to place an FP64 tap's significand for an exact sum.  The direct kernels keep
 // copies of the first kFxFields fields of the P set (u, v, w, e: the derivative pass's and the
 // Laplacians' taps); per family and axis, the masks choose the stencils they evaluate on the
-// copies.  The others stay the FP64 form's (kExact* above).
-constexpr int kFxFields = 4;
+// copies.  The others stay the FP64 form's (kExact* above).  Copies of the twelve flux fields as
+// well (kFxFields = NPF) with the flux divergences on them measured 5-7 % slower per 256^3 step:
+// writing twelve more copies costs more than their stencils save.
 constexpr int kFxDeriv = 0b111, kFxFlux = 0, kFxLap = 0b111;
 static_assert(kFxFlux == 0 || kFxFields == NPF, "flux stencils on copies need copies of every field");
 static_assert(PU < kFxFields && PV < kFxFields && PW < kFxFields && PT < kFxFields, "u, v, w, e have copies");
@@ -257,7 +258,7 @@ __device__ __noinline__ void deriv9_fallback(const R* pu, const R* pv, const R* 
 // fallbacks in the rare cell that needs one (the same bits either way).
 // NC = false reads the P set from L2 (ld_tap), for a launch whose other blocks write it.
 // FXT: a box that keeps a fixed-point copy of the P set (the kFxDeriv axes read the copy where it
-// is usable; the FP64 evaluation where it is not).
+// is usable and the step did not start from an upload; the FP64 evaluation otherwise).
 template <class R, bool NC = true, bool FXT = false>
 __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k, int stage) {
     const int pr = b.sc->pbase ^ ((stage - 1) & 1);
@@ -270,7 +271,8 @@ __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k
     const R* pw = P + PW * fs + c;
     R d[9];
     if constexpr (sizeof(R) == 8 && FXT) {
-        const bool usable = !b.sc->fx_bad[pr];
+        // the first stage after an upload reads the FP64 fields (fx_fresh)
+        const bool usable = !b.sc->fx_bad[pr] && !(stage == 1 && b.sc->fx_fresh);
         bool xf = !usable;
         if (usable) {
             const long long* X = b.X[pr];

@@ -1295,8 +1295,9 @@ cudaError_t tma_encode_maps(const BoxView& v, void* out) {
     const int sshape[4] = {BX_I, BX_J, BX_K, BX_C};
     for (int q = 0; q < 4; q++)
         if (!one(&m->s[q], v.S, NSF, sshape[q])) return cudaErrorInvalidValue;
-    // the fixed-point copies: the P sets' geometry, 64-bit integer words
-    for (int set = 0; set < 2 && fp64 && v.X[0]; set++)
+    // the fixed-point copies of every field (CNS_ASSEMBLE_TMA_FX): the P sets' geometry, 64-bit
+    // integer words
+    for (int set = 0; set < 2 && fp64 && v.X[0] && v.fx == NPF; set++)
         for (int sh = 0; sh < 7; sh++) {
             const cuuint64_t dims[4] = {g2, g1, g0, (cuuint64_t)NPF};
             const cuuint64_t strides[3] = {(cuuint64_t)v.sj * 8, (cuuint64_t)v.si * 8, (cuuint64_t)v.fs * 8};

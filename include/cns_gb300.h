@@ -261,9 +261,9 @@ int cns_box_set_tile(cns_box *box, const int tlog[3]);
  * exactly on the integer pipes reading the same fixed-point copies instead of placing each FP64
  * tap's significand; within ~2e-15 of the direct kernel, not bit-identical).
  * DIRECT, TMA and TMA_WS give identical bits.  A new mixed box starts on a TMA kernel when the
- * driver provides the tensor-map encoder; a new FP64 box on the direct kernel, which is the
- * faster one for FP64 on GB300 (the FP64 pipe, not the loads, sets its time).  The autotuner
- * keeps an FP64 box's kernel. */
+ * driver provides the tensor-map encoder; a new FP64 box on CNS_ASSEMBLE_FX, the fastest for FP64
+ * on GB300 (the FP64 pipe, not the loads, sets the time of the FP64 kernels; the copies take
+ * 64 bytes a cell in the box's memory).  The autotuner keeps an FP64 box's kernel. */
 enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2, CNS_ASSEMBLE_TMA_FX = 3,
        CNS_ASSEMBLE_FX = 4 };
 int cns_box_get_kernel(const cns_box *box, int *kernel);

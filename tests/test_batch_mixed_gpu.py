@@ -148,7 +148,7 @@ def test_autotune_keeps_results_and_state(gpu, cns):
     box = cns.Box(24, I.box_dx(24), I.CFL, I.ETA, I.ALAM)
     box.upload(I.initial_state(24, perturb=1e-3, seed=3))
     t, k, ms = box.autotune(trial_steps=1)
-    assert (sum(t) == 8 or t == (-1, 0, 0)) and k == 0 and ms > 0
+    assert (sum(t) == 8 or t == (-1, 0, 0)) and k == cns.CNS_ASSEMBLE_FX and ms > 0  # FP64 keeps its kernel
     box.advance(2)
     other = cns.Box(24, I.box_dx(24), I.CFL, I.ETA, I.ALAM)
     other.upload(I.initial_state(24, perturb=1e-3, seed=3))
@@ -244,7 +244,7 @@ def test_fp64_tma_assembly_equals_direct(gpu, cns, n, ties):
     for kern in (cns.CNS_ASSEMBLE_DIRECT, cns.CNS_ASSEMBLE_TMA):
         b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
         try:
-            assert b.kernel() == cns.CNS_ASSEMBLE_DIRECT
+            assert b.kernel() == cns.CNS_ASSEMBLE_FX  # a new FP64 box's kernel
             b.set_kernel(kern)
             b.upload(I.initial_state(n, **kw))
             b.advance(4)
