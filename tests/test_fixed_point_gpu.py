@@ -116,3 +116,18 @@ def test_switching_between_the_fixed_point_kernels_between_steps(gpu, cns, oracl
         with pytest.raises(cns.CnsError):
             m.set_kernel(k)
     m.close()
+
+
+@pytest.mark.parametrize("amp", [(1.0, 0.0, 0.0), (1e-6, 1.0, 1e-3), (0.0, 0.0, 0.0)])
+def test_fixed_point_copies_of_fields_that_start_at_zero_or_differ_in_scale(gpu, cns, oracle, amp):
+    """Velocity components that start at zero (their exponents then come from nothing, and the
+    first values written do not fit: the kernels fall back to the FP64 fields until the maxima
+    catch up) or differ by six orders of magnitude (one exponent per field): the default kernels
+    stay within the FP64 bar of the oracle and within 1e-13 of the FP64-tap kernels."""
+    n, steps = (24, 20, 28), 6
+    U0 = I.initial_state(n, amp=amp, perturb=1e-3, seed=44)
+    ref, _ = oracle.advance(U0, steps, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    fx, _ = run(cns, n, U0, steps, cns.CNS_ASSEMBLE_FX)
+    assert normwise(fx, ref).max() <= FP64_TOL
+    direct, _ = run(cns, n, U0, steps, cns.CNS_ASSEMBLE_DIRECT)
+    assert normwise(fx, direct).max() <= 1e-13
