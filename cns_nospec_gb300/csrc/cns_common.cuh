@@ -84,7 +84,8 @@ struct BoxScalars {
     // The plain form's fixed-point copies of the P sets (cns_exact.cuh): fx_bad[s] != 0 when the
     // copy of P[s] is unusable (not written, or a value did not fit its exponent), fx_e[s][f] the
     // exponent of field f in it; fx_prev[f] / fx_cur[f] the largest biased exponent field of P
-    // field f over the previous step's writes / the writes since.  fx_restore: the box was just
+    // field f over the previous step's tracked writes / those since (the direct kernels track
+    // stage 3's writes, the TMA kernel every stage's; an upload, the uploaded set).  fx_restore: the box was just
     // restored with its exponents (the conversion after the upload keeps fx_e, and fx_prev stays).
     // fx_fresh: the copy was made from an upload (not written by a step) and the step after it
     // has not ended; that step's first derivative pass reads the FP64 fields, as the upload fused

@@ -141,7 +141,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
             }
             if (STAGE == 3 && b.host_out) store_host(b, i, j, k, un);
             if (kPlainFx) {
-                FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false, kFxFields};
+                // the maxima of stage 3's writes only (the step's result; the next step's stages
+                // differ from it by one step's change, well inside the exponents' 4x headroom):
+                // tracking every stage measured 1 % of the step
+                FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false, kFxFields, STAGE == 3};
                 epilogue_plain(b, (double*)Pw, c, i, j, k, un, &health, &cq, &sink);
                 fx_bad |= sink.bad;
                 if (kDefer) {

@@ -406,13 +406,14 @@ struct FxSink {
     const int* E;
     int* s_emax;
     bool bad;
-    int nf;  // fields with a copy: the first nf of the set
+    int nf;      // fields with a copy: the first nf of the set
+    bool track;  // fold the written values into the block's maxima
 };
 __device__ __forceinline__ void fx_store(FxSink& fx, const BoxView& b, long long c, int i, int j, int k, int f,
                                          double v, int mask) {
     const long long w = fx_word(v, fx.E[f], &fx.bad);
     store_img(fx.X + f * b.fs, b, c, i, j, k, w, mask);
-    fx_track(fx.s_emax + f, fx_efield(v));
+    if (fx.track) fx_track(fx.s_emax + f, fx_efield(v));
 }
 
 // The block's maxima and overflow for box `bx` (set W written) into the box's scalars, and the

@@ -978,7 +978,7 @@ __global__ void __launch_bounds__(2 * kTileThreads, 1) k_assemble_fx(const BoxVi
             stash[(i * 5 + 4) * kTileThreads + tid] = de[i];
         }
         if (!usable || x.xf) assemble_column_fp64(b, T, j, k, STAGE, stash, tid, ci0, ci1);
-        FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false, NPF};
+        FxSink sink{b.X[pr ^ 1], b.sc->fx_e[pr ^ 1], s_emax, false, NPF, true};
         write_back_fx<STAGE>(b, T, stash, tid, tj, tk, ci0, ci1, &sink);
         fx_bad |= sink.bad;
         __syncthreads();  // the stash buffer receives load g + 1, issued at the top of the next tile
