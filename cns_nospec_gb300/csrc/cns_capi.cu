@@ -243,6 +243,9 @@ static void fill_coefs(BoxView& v, const cns_box_desc* d) {
     }
     c.eta = d->eta;
     cast_coefs(v.c32, v.c64);
+    // the merged Laplacian sums (u: j + k, v: i + k, w: i + j, e: all three) need equal factors
+    v.lap_merge = c.vl[0][1][4] == c.vl[0][2][4] && c.vl[1][0][4] == c.vl[1][2][4] &&
+                  c.vl[2][0][4] == c.vl[2][1][4] && c.tl[0][4] == c.tl[1][4] && c.tl[1][4] == c.tl[2][4];
 }
 
 // ---- boxes -------------------------------------------------------------------------------
@@ -558,6 +561,8 @@ struct WorkLists {
     int ndfx64 = 0;
     const Tile* afx64 = nullptr;  // FP64 boxes on the direct assembly on fixed-point taps
     int nafx64 = 0;
+    const Tile* afxm64 = nullptr;  // the same, boxes whose Laplacians take the merged sums
+    int nafxm64 = 0;
 };
 
 // One RK3 step of the boxes behind `views`.  When `ev` is given, an event is recorded after
@@ -599,6 +604,10 @@ static int enqueue_step(const BoxView* views, int nviews, const WorkLists& w, cu
         }
         if (w.nafx64) {
             CK(launch_assemble(kFormPlainFx, views, w.afx64, w.nafx64, stage, st));
+            if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
+        }
+        if (w.nafxm64) {
+            CK(launch_assemble(kFormPlainFxMerge, views, w.afxm64, w.nafxm64, stage, st));
             if ((rc = mark(CNS_KERN_ASSEMBLE))) return rc;
         }
         if (w.nx64) {
@@ -644,6 +653,8 @@ static WorkLists box_lists(const cns_box* b) {
             w.x64 = b->d_xtiles, w.nx64 = b->nxtiles;
         else if (b->kernel == CNS_ASSEMBLE_TMA_FX)
             w.f64 = b->d_xtiles, w.nf64 = b->nxtiles;
+        else if (b->kernel == CNS_ASSEMBLE_FX && b->view.lap_merge)
+            w.afxm64 = b->d_tiles, w.nafxm64 = b->ntiles;
         else if (b->kernel == CNS_ASSEMBLE_FX)
             w.afx64 = b->d_tiles, w.nafx64 = b->ntiles;
         else
@@ -882,7 +893,7 @@ extern "C" int cns_batch_size(const cns_batch* bt) { return bt ? (int)bt->member
 static int batch_rebuild(cns_batch* bt, bool capture = true) {
     CK(cudaStreamSynchronize(bt->stream));
     std::vector<BoxView> views;
-    std::vector<Tile> d64, a64, f64, d32, a32, x32, w32, dx32, dfx64, afx64;  // the lists of WorkLists
+    std::vector<Tile> d64, a64, f64, d32, a32, x32, w32, dx32, dfx64, afx64, afxm64;  // the lists of WorkLists
     for (size_t m = 0; m < bt->members.size(); m++) {
         const cns_box* b = bt->members[m];
         views.push_back(b->view);
@@ -892,7 +903,8 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
             if (b->kernel == CNS_ASSEMBLE_TMA_FX)
                 append_xtiles(b->desc.n, (int)m, f64);
             else
-                append_tiles(b->desc.n, b->view.tlog, (int)m, b->kernel == CNS_ASSEMBLE_FX ? afx64 : a64);
+                append_tiles(b->desc.n, b->view.tlog, (int)m,
+                             b->kernel != CNS_ASSEMBLE_FX ? a64 : b->view.lap_merge ? afxm64 : afx64);
             continue;
         }
         if (b->kernel == CNS_ASSEMBLE_TMA || b->kernel == CNS_ASSEMBLE_TMA_WS) {
@@ -905,8 +917,8 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     }
     std::vector<Tile> all;
     all.reserve(d64.size() + a64.size() + f64.size() + d32.size() + a32.size() + x32.size() + w32.size() + dx32.size() +
-                dfx64.size() + afx64.size());
-    for (auto* v : {&d64, &a64, &f64, &d32, &a32, &x32, &w32, &dx32, &dfx64, &afx64})
+                dfx64.size() + afx64.size() + afxm64.size());
+    for (auto* v : {&d64, &a64, &f64, &d32, &a32, &x32, &w32, &dx32, &dfx64, &afx64, &afxm64})
         all.insert(all.end(), v->begin(), v->end());
     const size_t nt = all.size();
     if (views.size() > bt->cap_views) {
@@ -935,7 +947,8 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
     w.w32 = at, w.nw32 = (int)w32.size(), at += w32.size();
     w.dx32 = at, w.ndx32 = (int)dx32.size(), at += dx32.size();
     w.dfx64 = at, w.ndfx64 = (int)dfx64.size(), at += dfx64.size();
-    w.afx64 = at, w.nafx64 = (int)afx64.size();
+    w.afx64 = at, w.nafx64 = (int)afx64.size(), at += afx64.size();
+    w.afxm64 = at, w.nafxm64 = (int)afxm64.size();
     bt->nviews = (int)views.size();
     if (bt->gexec) {
         cudaGraphExecDestroy(bt->gexec);

@@ -129,6 +129,8 @@ struct BoxView {
                             // P[1] (the P sets' geometry, fields fs apart)
     int fx;                 // fields with copies: 0 (none), kFxFields (CNS_ASSEMBLE_FX) or NPF
                             // (CNS_ASSEMBLE_TMA_FX)
+    int lap_merge;          // the Laplacians' factors are equal where the merged sums need it
+                            // (cubic cells: v_yy's and w_zz's 4/3 apart)
 };
 // The fields the direct kernels keep fixed-point copies of: u, v, w, e (the derivative pass's and
 // the Laplacians' taps; PU..PT).

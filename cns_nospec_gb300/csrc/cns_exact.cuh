@@ -238,8 +238,7 @@ __host__ __device__ __forceinline__ void fx_tap(long long& L, long long& H, long
 // sum_{m=1..4} w_m (X(m) + SGN X(-m)) of fixed-point words, rounded once to FP64 and scaled by
 // 2^E; false when the result is outside FP64's normal range (then *out is unspecified).
 template <int W1, int W2, int W3, int W4, int SGN, class Ld>
-__host__ __device__ __forceinline__ bool fx_sum8(const Ld& ld, int E, double* out) {
-    long long L = 0, H = 0;
+__host__ __device__ __forceinline__ void fx_taps8(long long& L, long long& H, const Ld& ld) {
     fx_tap(L, H, ld(1), W1);
     fx_tap(L, H, ld(-1), SGN * W1);
     fx_tap(L, H, ld(2), W2);
@@ -248,6 +247,11 @@ __host__ __device__ __forceinline__ bool fx_sum8(const Ld& ld, int E, double* ou
     fx_tap(L, H, ld(-3), SGN * W3);
     fx_tap(L, H, ld(4), W4);
     fx_tap(L, H, ld(-4), SGN * W4);
+}
+template <int W1, int W2, int W3, int W4, int SGN, class Ld>
+__host__ __device__ __forceinline__ bool fx_sum8(const Ld& ld, int E, double* out) {
+    long long L = 0, H = 0;
+    fx_taps8<W1, W2, W3, W4, SGN>(L, H, ld);
     return xround(H, L, E, out);
 }
 
@@ -258,6 +262,29 @@ __host__ __device__ __forceinline__ double fx_d1acc(double acc, const Ld& ld, in
     double x;
     *fail |= !fx_sum8<672, -168, 32, -3, -1>(ld, E, &x);
     return fma(a[4], x, acc);
+}
+// Second differences of one field along two or three axes whose factors are equal (cubic
+// cells): the sum over all their taps formed exactly and rounded once (|S| < 2^(62+16)).
+template <class L1, class L2>
+__host__ __device__ __forceinline__ double fx_d2acc2(double acc, const L1& l1, const L2& l2, int E, const double* b,
+                                                     bool* fail) {
+    long long L = 0, H = 0;
+    fx_taps8<8064, -1008, 128, -9, 1>(L, H, l1);
+    fx_taps8<8064, -1008, 128, -9, 1>(L, H, l2);
+    double x;
+    *fail |= !xround(H, L, E, &x);
+    return fma(b[4], x, acc);
+}
+template <class L1, class L2, class L3>
+__host__ __device__ __forceinline__ double fx_d2acc3(double acc, const L1& l1, const L2& l2, const L3& l3, int E,
+                                                     const double* b, bool* fail) {
+    long long L = 0, H = 0;
+    fx_taps8<8064, -1008, 128, -9, 1>(L, H, l1);
+    fx_taps8<8064, -1008, 128, -9, 1>(L, H, l2);
+    fx_taps8<8064, -1008, 128, -9, 1>(L, H, l3);
+    double x;
+    *fail |= !xround(H, L, E, &x);
+    return fma(b[4], x, acc);
 }
 template <class Ld>
 __host__ __device__ __forceinline__ double fx_d2acc(double acc, const Ld& ld, int E, const double* b, bool* fail) {

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __rest
 // FXT: FP64 boxes that keep a fixed-point copy of the P set: the kFxLap / kFxFlux stencils read
 // the copy of the set read (where it is usable), and the write-back also writes the copy of the
 // set written, with the block's maxima of its fields (as k_assemble_fx).
-template <class R, int STAGE, bool FXT>
+template <class R, int STAGE, bool FXT, bool MRG = false>
 __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __restrict__ boxes,
                                                          const Tile* __restrict__ tiles, int ntiles) {
     pdl_enter();
@@ -105,8 +105,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
                 const bool usable = !b.sc->fx_bad[pr];
                 bool xf = !usable;
                 if (usable)
-                    assemble_terms<R, true, kFxLap, kFxFlux>(b, Pr, S, c, u0, v0, w0, t0, f, &xf, b.X[pr],
-                                                             b.sc->fx_e[pr]);
+                    assemble_terms<R, true, kFxLap, kFxFlux, MRG>(b, Pr, S, c, u0, v0, w0, t0, f, &xf, b.X[pr],
+                                                                  b.sc->fx_e[pr]);
                 if (xf) assemble_terms_fallback<R>(b, Pr, S, c, u0, v0, w0, t0, f);
             } else if constexpr (sizeof(R) == 8) {
                 bool xf = false;
@@ -305,16 +305,16 @@ static cudaError_t launch_deriv_t(const BoxView* boxes, const Tile* tiles, int n
     auto fn = k_deriv<R, FXT>;
     return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles, stage);
 }
-template <class R, bool FXT>
+template <class R, bool FXT, bool MRG = false>
 static cudaError_t launch_assemble_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (stage == 1) {
-        auto fn = k_assemble<R, 1, FXT>;
+        auto fn = k_assemble<R, 1, FXT, MRG>;
         return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else if (stage == 2) {
-        auto fn = k_assemble<R, 2, FXT>;
+        auto fn = k_assemble<R, 2, FXT, MRG>;
         return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else {
-        auto fn = k_assemble<R, 3, FXT>;
+        auto fn = k_assemble<R, 3, FXT, MRG>;
         return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     }
 }
@@ -334,6 +334,7 @@ cudaError_t launch_assemble(int form, const BoxView* boxes, const Tile* tiles, i
     if (ntiles <= 0) return cudaSuccess;
     if (form == kFormMixed) return launch_assemble_t<float, false>(boxes, tiles, ntiles, stage, st);
     if (form == kFormPlainFx) return launch_assemble_t<double, true>(boxes, tiles, ntiles, stage, st);
+    if (form == kFormPlainFxMerge) return launch_assemble_t<double, true, true>(boxes, tiles, ntiles, stage, st);
     return launch_assemble_t<double, false>(boxes, tiles, ntiles, stage, st);
 }
 cudaError_t launch_refs(const BoxView* boxes, int nboxes, cudaStream_t st) {

@@ -298,8 +298,10 @@ __device__ __forceinline__ void deriv_cell(const BoxView& b, int i, int j, int k
 // diffterm + hypterm of one cell (cpu/diffterm.cpp:155-311, cpu/hypterm.cpp:29-208) from the P set
 // Pr and the S set at element c: f[l] = D[l] + F[l].  NB as in d1.
 // FXL / FXF: masks of the Laplacian / flux-divergence axes read from the fixed-point copy Xr of
-// the P set (exponents XE); 0 without a copy.
-template <class R, bool NB, int FXL = 0, int FXF = 0>
+// the P set (exponents XE); 0 without a copy.  MRG (FXL = all axes, a box whose Laplacian factors
+// are equal on the axes merged, lap_merge): the second differences of a field that share a
+// factor form one exact sum and one rounding (u: j + k; v: i + k; w: i + j; e: all three).
+template <class R, bool NB, int FXL = 0, int FXF = 0, bool MRG = false>
 __device__ __forceinline__ void assemble_terms(const BoxView& b, const R* __restrict__ Pr, const R* __restrict__ S,
                                                long long c, R u0, R v0, R w0, R t0, R (&f)[5], bool* xf,
                                                const long long* Xr = nullptr, const int* XE = nullptr) {
@@ -314,26 +316,40 @@ __device__ __forceinline__ void assemble_terms(const BoxView& b, const R* __rest
     auto xat = [&](int f) -> const long long* { return (XL || XF) ? Xr + f * fs + c : nullptr; };
     auto xe = [&](int f) -> int { return (XL || XF) ? XE[f] : 0; };
     // diffterm momentum components (cpu/diffterm.cpp:155-269)
-    R dmx = cf.vc[0] * u0;
-    dmx = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmx, pu, xat(PU), xe(PU), si, cf.vl[0][0], xf);
-    dmx = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmx, pu, xat(PU), xe(PU), sj, cf.vl[0][1], xf);
-    dmx = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmx, pu, xat(PU), xe(PU), 1, cf.vl[0][2], xf);
-    dmx = d1acc<xon(kExactMixed, 0), R, NB, false>(dmx, S + SX * fs + c, si, cf.mx[0], xf);
-    R dmy = cf.vc[1] * v0;
-    dmy = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmy, pv, xat(PV), xe(PV), si, cf.vl[1][0], xf);
-    dmy = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmy, pv, xat(PV), xe(PV), sj, cf.vl[1][1], xf);
-    dmy = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmy, pv, xat(PV), xe(PV), 1, cf.vl[1][2], xf);
-    dmy = d1acc<xon(kExactMixed, 1), R, NB, false>(dmy, S + SY * fs + c, sj, cf.mx[1], xf);
-    R dmz = cf.vc[2] * w0;
-    dmz = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmz, pw, xat(PW), xe(PW), si, cf.vl[2][0], xf);
-    dmz = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmz, pw, xat(PW), xe(PW), sj, cf.vl[2][1], xf);
-    dmz = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmz, pw, xat(PW), xe(PW), 1, cf.vl[2][2], xf);
-    dmz = d1acc<xon(kExactMixed, 2), R, NB, false>(dmz, S + SZ * fs + c, 1, cf.mx[2], xf);
-    // diffterm energy component (cpu/diffterm.cpp:272-311)
+    R dmx = cf.vc[0] * u0, dmy = cf.vc[1] * v0, dmz = cf.vc[2] * w0;
     R de = fma(cf.tc, t0, __ldcg(S + SPHI * fs + c));
-    de = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(de, pt, xat(PT), xe(PT), si, cf.tl[0], xf);
-    de = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(de, pt, xat(PT), xe(PT), sj, cf.tl[1], xf);
-    de = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(de, pt, xat(PT), xe(PT), 1, cf.tl[2], xf);
+    if constexpr (MRG) {
+        static_assert(FXL == 0b111, "merged sums read every axis from the copy");
+        const XWords ui{xat(PU), si}, uj{xat(PU), sj}, uk{xat(PU), 1};
+        dmx = fx_d2acc(dmx, ui, xe(PU), cf.vl[0][0], xf);
+        dmx = fx_d2acc2(dmx, uj, uk, xe(PU), cf.vl[0][1], xf);
+        const XWords vi{xat(PV), si}, vj{xat(PV), sj}, vk{xat(PV), 1};
+        dmy = fx_d2acc(dmy, vj, xe(PV), cf.vl[1][1], xf);
+        dmy = fx_d2acc2(dmy, vi, vk, xe(PV), cf.vl[1][0], xf);
+        const XWords wi{xat(PW), si}, wj{xat(PW), sj}, wk{xat(PW), 1};
+        dmz = fx_d2acc(dmz, wk, xe(PW), cf.vl[2][2], xf);
+        dmz = fx_d2acc2(dmz, wi, wj, xe(PW), cf.vl[2][0], xf);
+        const XWords ti{xat(PT), si}, tj{xat(PT), sj}, tk{xat(PT), 1};
+        de = fx_d2acc3(de, ti, tj, tk, xe(PT), cf.tl[0], xf);
+    } else {
+        dmx = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmx, pu, xat(PU), xe(PU), si, cf.vl[0][0], xf);
+        dmx = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmx, pu, xat(PU), xe(PU), sj, cf.vl[0][1], xf);
+        dmx = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmx, pu, xat(PU), xe(PU), 1, cf.vl[0][2], xf);
+        dmy = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmy, pv, xat(PV), xe(PV), si, cf.vl[1][0], xf);
+        dmy = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmy, pv, xat(PV), xe(PV), sj, cf.vl[1][1], xf);
+        dmy = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmy, pv, xat(PV), xe(PV), 1, cf.vl[1][2], xf);
+        dmz = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(dmz, pw, xat(PW), xe(PW), si, cf.vl[2][0], xf);
+        dmz = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(dmz, pw, xat(PW), xe(PW), sj, cf.vl[2][1], xf);
+        dmz = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(dmz, pw, xat(PW), xe(PW), 1, cf.vl[2][2], xf);
+        // diffterm energy component (cpu/diffterm.cpp:272-311)
+        de = tap_d2acc<xon(FXL, 0), xon(kExactLap, 0), R, NB>(de, pt, xat(PT), xe(PT), si, cf.tl[0], xf);
+        de = tap_d2acc<xon(FXL, 1), xon(kExactLap, 1), R, NB>(de, pt, xat(PT), xe(PT), sj, cf.tl[1], xf);
+        de = tap_d2acc<xon(FXL, 2), xon(kExactLap, 2), R, NB>(de, pt, xat(PT), xe(PT), 1, cf.tl[2], xf);
+    }
+    // the mixed viscous terms (cpu/diffterm.cpp:177-265)
+    dmx = d1acc<xon(kExactMixed, 0), R, NB, false>(dmx, S + SX * fs + c, si, cf.mx[0], xf);
+    dmy = d1acc<xon(kExactMixed, 1), R, NB, false>(dmy, S + SY * fs + c, sj, cf.mx[1], xf);
+    dmz = d1acc<xon(kExactMixed, 2), R, NB, false>(dmz, S + SZ * fs + c, 1, cf.mx[2], xf);
     de = fma(dmx, u0, de);
     de = fma(dmy, v0, de);
     de = fma(dmz, w0, de);

@@ -28,8 +28,9 @@ cudaError_t launch_pdl(void (*fn)(Params...), dim3 grid, dim3 block, size_t smem
 int set_error(int code, const char* msg);
 
 // fused RK3 stage kernels (cns_fused.cu); precision / form 0 = FP64 stencils, 1 = FP32 stencils,
-// 2 = FP64 boxes that keep a fixed-point copy of the P set (part of the stencils on the copy)
-constexpr int kFormPlain = 0, kFormMixed = 1, kFormPlainFx = 2;
+// 2 = FP64 boxes that keep a fixed-point copy of the P set (part of the stencils on the copy),
+// 3 = the same with the Laplacians' merged sums (boxes with lap_merge; assembly only)
+constexpr int kFormPlain = 0, kFormMixed = 1, kFormPlainFx = 2, kFormPlainFxMerge = 3;
 cudaError_t launch_prim(int precision, const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st);
 cudaError_t launch_deriv(int form, const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st);
 cudaError_t launch_assemble(int form, const BoxView* boxes, const Tile* tiles, int ntiles, int stage,

@@ -34,10 +34,11 @@ def model_word(u, E):
     return ((hi & 0xFFFFFFFF) << 32) | lo, False
 
 
-def model_sum(words, w, sgn, E):
-    """The rounded sum of the eight words (None outside FP64's normal range)."""
+def model_sum(words, w, sgn, E, weights_given=False):
+    """The rounded sum of the words (None outside FP64's normal range): eight words with the
+    weights w at +m and sgn * w at -m, or with weights_given, any words with the weights w."""
     S = 0
-    for word, wm in zip(words, list(w) + [sgn * x for x in w]):
+    for word, wm in zip(words, list(w) if weights_given else list(w) + [sgn * x for x in w]):
         lo, hi = word & 0xFFFFFFFF, word >> 32
         hi = hi - (1 << 32) if hi >= 1 << 31 else hi
         S += wm * (hi * (1 << 31) + lo)
@@ -116,6 +117,31 @@ def test_fixed_point_words_and_sums_match_the_model(driver):
             else:
                 assert ok == "1" and int(b, 16) == want, (E, taps, w)
     assert 0 < flagged < len(cs) // 2
+
+
+def test_merged_second_difference_sums_match_the_model(driver):
+    """fx_d2acc2 / fx_d2acc3 (the Laplacians of cubic cells): one exact sum over the taps of two or
+    three stencils, rounded once; here the words as given, mirrored and rotated."""
+    cs = cases(6000, seed=23)
+    lines = run(driver, cs)
+    checked = 0
+    for (E, taps), line in zip(cs, lines):
+        f = line.split()
+        if f[8] == "1":
+            continue
+        words = [int(x, 16) for x in f[:8]]
+        plus, minus = words[:4], words[4:]
+        mirrored = minus + plus
+        rotated = plus[1:] + plus[:1] + minus[1:] + minus[:1]
+        ws = list(W2) + list(W2)
+        for ok, b, sets in ((f[13], f[14], (words, mirrored)), (f[15], f[16], (words, mirrored, rotated))):
+            want = model_sum([w for st in sets for w in st], ws * len(sets), 1, E, weights_given=True)
+            if want is None:
+                assert ok == "0"
+            else:
+                assert ok == "1" and int(b, 16) == want, (E, taps, len(sets))
+                checked += 1
+    assert checked > 3000
 
 
 def test_fixed_point_sums_are_within_the_stated_bound(driver):
