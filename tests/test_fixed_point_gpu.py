@@ -131,3 +131,21 @@ def test_fixed_point_copies_of_fields_that_start_at_zero_or_differ_in_scale(gpu,
     assert normwise(fx, ref).max() <= FP64_TOL
     direct, _ = run(cns, n, U0, steps, cns.CNS_ASSEMBLE_DIRECT)
     assert normwise(fx, direct).max() <= 1e-13
+
+
+def test_snapshot_taken_right_after_an_upload_resumes_bit_for_bit(gpu, cns, tmp_path):
+    """A snapshot of a freshly uploaded box carries that its first step reads the FP64 fields in
+    the derivative pass (as the upload fused with that pass does); resumed, it continues as the
+    box it was taken from, bit for bit."""
+    n = 32
+    U0 = I.initial_state(n, perturb=1e-3, seed=45)
+    a = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    a.upload(U0)
+    a.save(tmp_path / "fresh.bin")
+    a.advance(3)
+    b = cns.Box(n, I.box_dx(n), I.CFL, I.ETA, I.ALAM)
+    b.load(tmp_path / "fresh.bin")
+    b.advance(3)
+    assert np.array_equal(a.download().view(np.uint64), b.download().view(np.uint64))
+    a.close()
+    b.close()
