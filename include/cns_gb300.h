@@ -269,7 +269,8 @@ enum { CNS_ASSEMBLE_DIRECT = 0, CNS_ASSEMBLE_TMA = 1, CNS_ASSEMBLE_TMA_WS = 2, C
 int cns_box_get_kernel(const cns_box *box, int *kernel);
 int cns_box_set_kernel(cns_box *box, int kernel);
 /* Time trial_steps RK3 steps of the box on every candidate shape (the 12 rectangular ones and
- * the linear one; for mixed boxes, with each of the three assembly kernels) and keep the fastest; the box's state is restored afterwards, so the run
+ * the linear one; for mixed boxes, with each of the three assembly kernels), twice, and keep the
+ * candidate whose faster run is the fastest; the box's state is restored afterwards, so the run
  * continues bit for bit.  Blocks. */
 int cns_box_autotune(cns_box *box, int trial_steps, int tlog_out[3], int *kernel_out, double *best_ms_per_step);
 /* Same for a batch.  Policy p = shape + 14 * kernel: shape 0 = every member on its
