@@ -178,15 +178,6 @@ __host__ __device__ inline long long cell_off(const BoxView& b, int i, int j, in
     return (long long)(i + CNS_NG) * b.si + (long long)(j + CNS_NG) * b.sj + (k + CNS_NG);
 }
 
-// Programmatic dependent launch of the step kernels: each waits for its predecessor's grid to
-// complete (memory included) before it touches anything, then lets its successor launch, whose
-// blocks take the SMs this grid's blocks free as it drains.  A hardware wait on grid completion,
-// not a spin: it ends when the predecessor ends.  Without the launch attribute both are no-ops.
-__device__ __forceinline__ void pdl_enter() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 // Positive doubles order like their bit patterns; the Courant max uses integer atomics.
 __device__ inline unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 

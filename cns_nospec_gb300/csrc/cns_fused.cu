@@ -40,7 +40,6 @@ __global__ void __launch_bounds__(kTileThreads) k_prim(const BoxView* __restrict
 template <class R, bool FXT>
 __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __restrict__ boxes, const Tile* __restrict__ tiles,
                                                       int ntiles, int stage) {
-    pdl_enter();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Tile T = tiles[t];
         const BoxView& b = boxes[T.box];
@@ -63,7 +62,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_deriv(const BoxView* __rest
 template <class R, int STAGE, bool FXT, bool MRG = false>
 __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __restrict__ boxes,
                                                          const Tile* __restrict__ tiles, int ntiles) {
-    pdl_enter();
     __shared__ int s_emax[NPF];
     int fx_box = -1, fx_set = 0;
     bool fx_bad = false;
@@ -207,7 +205,6 @@ __global__ void k_refs(const BoxView* __restrict__ boxes, int nboxes) {
 
 // ---- k_stepend: dt for the next step from the Courant max (cpu/advance.cpp:52-58) ----------
 __global__ void k_stepend(const BoxView* __restrict__ boxes, int nboxes, int flip) {
-    pdl_enter();
     const int bx = blockIdx.x * blockDim.x + threadIdx.x;
     if (bx >= nboxes) return;
     BoxScalars* s = boxes[bx].sc;
@@ -303,19 +300,19 @@ static cudaError_t launch_prim_t(const BoxView* boxes, const Tile* tiles, int nt
 template <class R, bool FXT>
 static cudaError_t launch_deriv_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     auto fn = k_deriv<R, FXT>;
-    return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles, stage);
+    return launch_step(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles, stage);
 }
 template <class R, bool FXT, bool MRG = false>
 static cudaError_t launch_assemble_t(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
     if (stage == 1) {
         auto fn = k_assemble<R, 1, FXT, MRG>;
-        return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
+        return launch_step(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else if (stage == 2) {
         auto fn = k_assemble<R, 2, FXT, MRG>;
-        return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
+        return launch_step(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     } else {
         auto fn = k_assemble<R, 3, FXT, MRG>;
-        return launch_pdl(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
+        return launch_step(fn, grid_for((const void*)fn, ntiles), kTileThreads, 0, st, boxes, tiles, ntiles);
     }
 }
 
@@ -369,7 +366,7 @@ cudaError_t launch_fx_pass(bool convert, const BoxView* boxes, const Tile* tiles
 }
 cudaError_t launch_stepend(const BoxView* boxes, int nboxes, int flip, cudaStream_t st) {
     if (nboxes <= 0) return cudaSuccess;
-    return launch_pdl(k_stepend, (nboxes + 127) / 128, 128, 0, st, boxes, nboxes, flip);
+    return launch_step(k_stepend, (nboxes + 127) / 128, 128, 0, st, boxes, nboxes, flip);
 }
 
 }  // namespace cns

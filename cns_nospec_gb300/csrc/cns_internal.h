@@ -7,20 +7,17 @@
 
 namespace cns {
 
-// Launch a step kernel with programmatic stream serialization (see pdl_enter): it may start
-// while the previous kernel of the stream drains, and waits for it on the device.
+// Launch a step kernel in plain stream order.  Programmatic dependent launch (each kernel
+// waiting on the device for its predecessor, its successor launched early to take the SMs as
+// they drain) was measured again with the current kernels: without it a graph-replayed 256^3
+// step is 1-1.5 % faster in FP64, 3 % faster in the mixed form, and cns_new_advance 1 % faster.
 template <class... Params, class... Args>
-cudaError_t launch_pdl(void (*fn)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+cudaError_t launch_step(void (*fn)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, fn, args...);
 }
 

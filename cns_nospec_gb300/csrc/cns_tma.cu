@@ -612,7 +612,6 @@ template <class R, int STAGE>
 __global__ void __launch_bounds__(kTileThreads, sizeof(R) == 4 ? 2 : 1) k_assemble_tma(const BoxView* __restrict__ boxes,
                                                                                    const Tile* __restrict__ tiles,
                                                                                    int ntiles) {
-    pdl_enter();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     R* buf[2] = {(R*)smem_raw, (R*)smem_raw + kBufElems};
     uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(R));
@@ -908,7 +907,6 @@ __device__ __forceinline__ void write_back_fx(const BoxView& b, const Tile& T, d
 template <int STAGE>
 __global__ void __launch_bounds__(2 * kTileThreads, 1) k_assemble_fx(const BoxView* __restrict__ boxes,
                                                               const Tile* __restrict__ tiles, int ntiles) {
-    pdl_enter();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     double* buf[2] = {(double*)smem_raw, (double*)smem_raw + kBufElems};
     uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(double));
@@ -1012,7 +1010,6 @@ __device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 256;" :
 template <int STAGE>
 __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __restrict__ boxes,
                                                             const Tile* __restrict__ tiles, int ntiles) {
-    pdl_enter();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* buf = (float*)smem_raw;                                // kWsBufs field buffers
     float* stash = buf + kWsBufs * kBufElems;                     // kWsSlots stash slots
@@ -1106,7 +1103,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
 // so the two give the same bits.  Waits bounded as in k_assemble_tma.
 __global__ void __launch_bounds__(kTileThreads, 2) k_deriv_tma(const BoxView* __restrict__ boxes,
                                                             const Tile* __restrict__ tiles, int ntiles, int stage) {
-    pdl_enter();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* buf[2] = {(float*)smem_raw, (float*)smem_raw + kBufElems};
     uint64_t* bar = (uint64_t*)(smem_raw + 2 * kBufElems * sizeof(float));
@@ -1324,7 +1320,7 @@ static cudaError_t launch_tma_stage(const BoxView* boxes, const Tile* tiles, int
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;
     const int grid = ntiles < nsm * per ? ntiles : nsm * per;
-    return launch_pdl(fn, grid, kTileThreads, smem, st, boxes, tiles, ntiles);
+    return launch_step(fn, grid, kTileThreads, smem, st, boxes, tiles, ntiles);
 }
 
 cudaError_t launch_assemble_tma(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
@@ -1354,7 +1350,7 @@ static cudaError_t launch_fx_stage(const BoxView* boxes, const Tile* tiles, int 
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;
     const int grid = ntiles < nsm * per ? ntiles : nsm * per;
-    return launch_pdl(fn, grid, 2 * kTileThreads, smem, st, boxes, tiles, ntiles);
+    return launch_step(fn, grid, 2 * kTileThreads, smem, st, boxes, tiles, ntiles);
 }
 
 cudaError_t launch_assemble_fx(const BoxView* boxes, const Tile* tiles, int ntiles, int stage, cudaStream_t st) {
@@ -1383,7 +1379,7 @@ cudaError_t launch_deriv_tma(const BoxView* boxes, const Tile* tiles, int ntiles
     int grid = 0;
     cudaError_t e = launch_tma_grid(k_deriv_tma, kTileThreads, kTmaSmem, ntiles, &grid);
     if (e != cudaSuccess) return e;
-    return launch_pdl(k_deriv_tma, grid, kTileThreads, kTmaSmem, st, boxes, tiles, ntiles, stage);
+    return launch_step(k_deriv_tma, grid, kTileThreads, kTmaSmem, st, boxes, tiles, ntiles, stage);
 }
 
 constexpr size_t kWsSmem =
@@ -1401,7 +1397,7 @@ static cudaError_t launch_ws_stage(const BoxView* boxes, const Tile* tiles, int 
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorInvalidConfiguration;  // 512 threads x 128 registers and kWsSmem must fit
     const int grid = ntiles < nsm * per ? ntiles : nsm * per;
-    return launch_pdl(fn, grid, kWsThreads, kWsSmem, st, boxes, tiles, ntiles);
+    return launch_step(fn, grid, kWsThreads, kWsSmem, st, boxes, tiles, ntiles);
 }
 
 bool assemble_ws_fits() {
