@@ -198,12 +198,14 @@ __host__ __device__ __forceinline__ double xd2acc_nb(double acc, const Ld& ld, c
 
 // ---- fixed-point copies of the stencil fields ------------------------------------------------
 // The integer sums above place each tap's significand for every stencil that reads it (~20
-// integer instructions a tap).  The plain form's TMA-staged assembly instead reads a fixed-point
-// copy of each field its stencils read: X = trunc(v * 2^-E), one exponent E per field and box,
-// chosen so that |X| < 2^62, stored as two 31-bit chunks in one 64-bit word (low word X mod 2^31,
-// in [0, 2^31); high word X >> 31, signed).  A stencil is then two wide integer multiply-adds per
-// tap, with no placement, and S = sum_m w_m X_m is exact in two 64-bit accumulators (|w| sums to
-// at most 18418 < 2^15); it is rounded once to FP64 (xround) as S * 2^E.  Against the exact sum
+// integer instructions a tap).  The plain form's default kernels (the derivative pass and the
+// Laplacians: copies of u, v, w, e) and its TMA-staged fixed-point assembly (copies of every
+// field) instead read a fixed-point copy of the field: X = trunc(v * 2^-E), one exponent E per
+// field and box, chosen so that |X| < 2^62, stored as two 31-bit chunks in one 64-bit word (low
+// word X mod 2^31, in [0, 2^31); high word X >> 31, signed).  A stencil is then two wide integer
+// multiply-adds per tap, with no placement, and S = sum_m w_m X_m is exact in two 64-bit
+// accumulators (|w| sums to at most 18418 < 2^15 a stencil, 3 x 18418 < 2^16 for three merged
+// second differences); it is rounded once to FP64 (xround) as S * 2^E.  Against the exact sum
 // sum_m w_m v_m the result is within half an ulp of itself plus sum|w| * 2^E: with E set from the
 // field's largest magnitude M (M < 2^(E + 60)), within sum|w| * 2^-60 M.  The producer of a field
 // writes its copy; values that do not fit (|v| >= 2^(E + 62) by the exponent test, or not finite)
