@@ -144,6 +144,19 @@ static void default_tlog(const int n[3], int out[3]) {
     }
 }
 
+// The order the persistent kernels take a box's tiles in: its i-planes one band of j rows at a
+// time, the band as many rows as keep the stencils' window (the tile's planes and 4 on each side,
+// the band's rows, ~272 bytes of fields a cell in the plain form) within ~24 MB of L2.  At 256^3
+// the plain form's step is 3-4 % faster than in plain i-major order (16-32 rows, by tile shape;
+// 8 rows is too few), where the window of whole planes (~180 MB) overflows L2.  Small boxes are
+// one band.
+static int band_rows(const int n[3], int ti, int tj) {
+    const double window = 24e6 / ((double)n[2] * (ti + 2 * CNS_NG) * 272.0);
+    int rows = tj;
+    while (rows * 2 <= window && rows < n[1]) rows *= 2;
+    return rows;
+}
+
 static void append_tiles(const int n[3], const int tlog[3], int box_index, std::vector<Tile>& out) {
     if (tlog[0] == kLinearTile) {
         const long long nt = tile_count(n, tlog);
@@ -151,9 +164,11 @@ static void append_tiles(const int n[3], const int tlog[3], int box_index, std::
         return;
     }
     const int ti = 1 << tlog[0], tj = 1 << tlog[1], tk = 1 << tlog[2];
-    for (int i0 = 0; i0 < n[0]; i0 += ti)
-        for (int j0 = 0; j0 < n[1]; j0 += tj)
-            for (int k0 = 0; k0 < n[2]; k0 += tk) out.push_back(Tile{box_index, i0, j0, k0});
+    const int band = band_rows(n, ti, tj);
+    for (int jb = 0; jb < n[1]; jb += band)
+        for (int i0 = 0; i0 < n[0]; i0 += ti)
+            for (int j0 = jb; j0 < n[1] && j0 < jb + band; j0 += tj)
+                for (int k0 = 0; k0 < n[2]; k0 += tk) out.push_back(Tile{box_index, i0, j0, k0});
 }
 
 static Geometry geometry(const cns_box_desc* d) {
