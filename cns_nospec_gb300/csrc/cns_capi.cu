@@ -146,25 +146,27 @@ static void default_tlog(const int n[3], int out[3]) {
 
 // The order the persistent kernels take a box's tiles in: its i-planes one band of j rows at a
 // time, the band as many rows as keep the stencils' window (the tile's planes and 4 on each side,
-// the band's rows, ~272 bytes of fields a cell in the plain form) within ~24 MB of L2.  At 256^3
-// the plain form's step is 3-4 % faster than in plain i-major order (16-32 rows, by tile shape;
-// 8 rows is too few), where the window of whole planes (~180 MB) overflows L2.  Small boxes are
-// one band.
-static int band_rows(const int n[3], int ti, int tj) {
-    const double window = 24e6 / ((double)n[2] * (ti + 2 * CNS_NG) * 272.0);
+// the band's rows, the fields a cell carries: ~272 bytes in the plain form, ~160 in the mixed)
+// within ~24 MB of L2.  At 256^3 the plain form's step is 3-4 % faster than in plain i-major
+// order (16-32 rows, by tile shape; 8 rows is too few), where the window of whole planes
+// (~180 MB) overflows L2, and the mixed form's 0.7 %.  Small boxes are one band.
+static int cell_bytes(int precision) { return precision == CNS_MIXED ? 160 : 272; }
+static int band_rows(const int n[3], int ti, int tj, int bytes) {
+    const double window = 24e6 / ((double)n[2] * (ti + 2 * CNS_NG) * bytes);
     int rows = tj;
     while (rows * 2 <= window && rows < n[1]) rows *= 2;
     return rows;
 }
 
-static void append_tiles(const int n[3], const int tlog[3], int box_index, std::vector<Tile>& out) {
+static void append_tiles(const int n[3], const int tlog[3], int box_index, std::vector<Tile>& out,
+                         int bytes = 272) {
     if (tlog[0] == kLinearTile) {
         const long long nt = tile_count(n, tlog);
         for (long long t = 0; t < nt; t++) out.push_back(Tile{box_index, 0, 0, (int)t});
         return;
     }
     const int ti = 1 << tlog[0], tj = 1 << tlog[1], tk = 1 << tlog[2];
-    const int band = band_rows(n, ti, tj);
+    const int band = band_rows(n, ti, tj, bytes);
     for (int jb = 0; jb < n[1]; jb += band)
         for (int i0 = 0; i0 < n[0]; i0 += ti)
             for (int j0 = jb; j0 < n[1] && j0 < jb + band; j0 += tj)
@@ -207,12 +209,14 @@ static Geometry geometry(const cns_box_desc* d) {
     return g;
 }
 
-static void append_xtiles(const int n[3], int box_index, std::vector<Tile>& out) {
+static void append_xtiles(const int n[3], int box_index, std::vector<Tile>& out, int bytes = 272) {
     int xi, xj, xk;
     tma_tile_shape(&xi, &xj, &xk);
-    for (int i0 = 0; i0 < n[0]; i0 += xi)
-        for (int j0 = 0; j0 < n[1]; j0 += xj)
-            for (int k0 = 0; k0 < n[2]; k0 += xk) out.push_back(Tile{box_index, i0, j0, k0});
+    const int band = band_rows(n, xi, xj, bytes);
+    for (int jb = 0; jb < n[1]; jb += band)
+        for (int i0 = 0; i0 < n[0]; i0 += xi)
+            for (int j0 = jb; j0 < n[1] && j0 < jb + band; j0 += xj)
+                for (int k0 = 0; k0 < n[2]; k0 += xk) out.push_back(Tile{box_index, i0, j0, k0});
 }
 
 template <class R>
@@ -354,7 +358,7 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
     }
     default_tlog(desc->n, v.tlog);
     std::vector<Tile> tiles;
-    append_tiles(desc->n, v.tlog, 0, tiles);
+    append_tiles(desc->n, v.tlog, 0, tiles, cell_bytes(desc->precision));
     b->ntiles = (int)tiles.size();
     std::vector<Tile> xtiles;
     std::vector<unsigned char> maps;
@@ -362,7 +366,7 @@ extern "C" int cns_box_create(const cns_box_desc* desc, cns_box** out) {
         // the TMA assemblies need the box's tensor maps; without a driver entry point for them
         // the box stays on the direct kernel
         b->d_xtiles = (Tile*)(b->arena + g.off_xtiles);
-        append_xtiles(desc->n, 0, xtiles);
+        append_xtiles(desc->n, 0, xtiles, cell_bytes(desc->precision));
         b->nxtiles = (int)xtiles.size();
         maps.resize(tma_maps_bytes());
         if (tma_encode_maps(v, maps.data()) == cudaSuccess) {
@@ -923,11 +927,11 @@ static int batch_rebuild(cns_batch* bt, bool capture = true) {
             continue;
         }
         if (b->kernel == CNS_ASSEMBLE_TMA || b->kernel == CNS_ASSEMBLE_TMA_WS) {
-            append_xtiles(b->desc.n, (int)m, dx32);
-            append_xtiles(b->desc.n, (int)m, b->kernel == CNS_ASSEMBLE_TMA ? x32 : w32);
+            append_xtiles(b->desc.n, (int)m, dx32, cell_bytes(CNS_MIXED));
+            append_xtiles(b->desc.n, (int)m, b->kernel == CNS_ASSEMBLE_TMA ? x32 : w32, cell_bytes(CNS_MIXED));
         } else {
-            append_tiles(b->desc.n, b->view.tlog, (int)m, d32);
-            append_tiles(b->desc.n, b->view.tlog, (int)m, a32);
+            append_tiles(b->desc.n, b->view.tlog, (int)m, d32, cell_bytes(CNS_MIXED));
+            append_tiles(b->desc.n, b->view.tlog, (int)m, a32, cell_bytes(CNS_MIXED));
         }
     }
     std::vector<Tile> all;
@@ -1227,7 +1231,7 @@ struct HostOutGuard {
 static int upload_first_step(cns_box* b, double* h_map, bool ghosts) {
     if (!b->d_queue || memcmp(b->queue_tlog, b->view.tlog, sizeof b->queue_tlog) != 0) {
         std::vector<Tile> tiles;
-        append_tiles(b->desc.n, b->view.tlog, 0, tiles);
+        append_tiles(b->desc.n, b->view.tlog, 0, tiles, cell_bytes(b->desc.precision));
         const std::vector<int> q = upload_deriv_queue(b->desc.n, b->view.tlog, tiles);
         CK(cudaStreamSynchronize(b->stream));
         cudaFree(b->d_queue);
@@ -1481,7 +1485,7 @@ static int apply_tile(cns_box* b, const int tlog[3]) {
     if (b->batch) CK(cudaStreamSynchronize(batch_stream(b->batch)));
     for (int a = 0; a < 3; a++) b->view.tlog[a] = tlog[a];
     std::vector<Tile> tiles;
-    append_tiles(b->desc.n, tlog, 0, tiles);
+    append_tiles(b->desc.n, tlog, 0, tiles, cell_bytes(b->desc.precision));
     b->ntiles = (int)tiles.size();
     CK(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b->d_view, &b->view, sizeof(BoxView), cudaMemcpyHostToDevice));
