@@ -113,6 +113,28 @@ def test_advance_noncubic_matches_oracle(gpu, cns, oracle, n):
     assert np.allclose(dts, rdt, rtol=1e-13, atol=0)
 
 
+@pytest.mark.parametrize("tile", [(3, 1, 4), (1, 3, 4), (2, 2, 4)])
+def test_banded_tile_walk_matches_oracle(gpu, cns, oracle, tile):
+    """A box long enough in k for its tiles to be walked in several bands of j rows, the last one
+    partial (200 rows in bands of 16 or 32), in both forms, against the oracle; the band sizes
+    follow the tile shape."""
+    n = (12, 200, 264)
+    U0 = I.initial_state(n, perturb=1e-3, seed=6)
+    dx = I.box_dx(n)
+    ref, _ = oracle.advance(U0, 2, dx, I.CFL, I.ETA, I.ALAM)
+    for prec, tol in ((cns.CNS_FP64, FP64_TOL), (cns.CNS_MIXED, MIXED_TOL)):
+        box = cns.Box(n, dx, I.CFL, I.ETA, I.ALAM, precision=prec)
+        try:
+            box.set_tile(tile)
+            box.upload(U0)
+            box.advance(2)
+            box.sync()
+            err = normwise(box.download(), ref)
+        finally:
+            box.close()
+        assert err.max() <= tol, (prec, tile, err)
+
+
 def test_advance_perturbed_128cube_100_steps(gpu, cns, oracle):
     """128^3, perturbed field, 100 RK3 steps against the oracle run live."""
     n = 128
