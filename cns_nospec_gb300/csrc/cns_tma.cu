@@ -41,11 +41,13 @@ static_assert(sizeof(CUtensorMap) == 128, "CUtensorMap is 128 bytes");
 struct Load {
     unsigned char set, field, shape;
 };
-__constant__ Load kSched[20] = {{1, SPHI, BX_C},   {0, PT, BX_FULL}, {0, PU, BX_FULL},  {1, SX, BX_I},
-                                {0, PV, BX_FULL}, {1, SY, BX_J},    {0, PW, BX_FULL},  {1, SZ, BX_K},
-                                {0, PMX, BX_I},   {0, PMY, BX_J},   {0, PMZ, BX_K},    {0, PFUU, BX_I},
-                                {0, PFUV, BX_IJ}, {0, PFUW, BX_IK}, {0, PFVV, BX_J},   {0, PFVW, BX_JK},
-                                {0, PFWW, BX_K},  {0, PHU, BX_I},   {0, PHV, BX_J},    {0, PHW, BX_K}};
+#define CNS_TMA_SCHED                                                                       \
+    {{1, SPHI, BX_C},  {0, PT, BX_FULL},   {0, PU, BX_FULL},   {1, SX, BX_I},   {0, PV, BX_FULL}, \
+     {1, SY, BX_J},    {0, PW, BX_FULL},   {1, SZ, BX_K},      {0, PMX, BX_I},  {0, PMY, BX_J},   \
+     {0, PMZ, BX_K},   {0, PFUU, BX_I},    {0, PFUV, BX_IJ},   {0, PFUW, BX_IK}, {0, PFVV, BX_J}, \
+     {0, PFVW, BX_JK}, {0, PFWW, BX_K},    {0, PHU, BX_I},     {0, PHV, BX_J},  {0, PHW, BX_K}}
+__constant__ Load kSched[20] = CNS_TMA_SCHED;
+constexpr Load kSchedPlan[20] = CNS_TMA_SCHED;  // the same list, for compile-time planning
 constexpr int kLoads = 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -988,11 +990,11 @@ __global__ void __launch_bounds__(2 * kTileThreads, 1) k_assemble_fx(const BoxVi
 // One 512-thread block per SM: warps 0-7 (the stencil group) run the 20 TMA-fed field phases of
 // tile t while warps 8-15 (the write-back group) run the FP64 write-back of tile t-1, so the
 // FP32 stencils and the FP64 write-back overlap instead of alternating.  The fields are
-// double-buffered, and the sums move between the groups through one 40 KB stash slot: full
-// (256 stencil arrivals) hands it to the write-back group, empty (256 write-back arrivals)
-// hands it back.  120 KB of shared memory leave the most L1 for the write-back's state loads:
-// a second slot (160 KB) measured 0.5-1 % slower, and a third field buffer with two slots
-// (200 KB) 10-15 % slower; the code takes any kWsBufs / kWsSlots.  The stencil group
+// staged in an 80 KB ring (below), and the sums move between the groups through one 40 KB stash
+// slot: full (256 stencil arrivals) hands it to the write-back group, empty (256 write-back
+// arrivals) hands it back.  120 KB of shared memory leave the most L1 for the write-back's state
+// loads: a second slot (160 KB) measured 0.5-1 % slower, and a third 40 KB field buffer with two
+// slots (200 KB) 10-15 % slower; the code takes any kWsSlots.  The stencil group
 // synchronises on named barrier 1 only (once per field); the write-back group needs no barrier.
 // Every wait is bounded.  A stencil thread whose wait gives up stops waiting and computing but
 // keeps taking part in the barrier and the hand-over, so no thread is ever left waiting on it;
@@ -1003,23 +1005,54 @@ constexpr int kWsThreads = 2 * kTileThreads;
 constexpr int kStashElems = 5 * XI * kTileThreads;  // 10240 floats
 static_assert(kStashElems == kBufElems, "a stash slot is one field buffer in size");
 
-constexpr int kWsBufs = 2;   // field buffers
 constexpr int kWsSlots = 1;  // stash slots
 __device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// The stencil group's field buffers are one ring of 80 KB in which each of a tile's 20 loads has
+// a fixed place (`off`, in floats, 512-byte aligned), the same in every tile.  A load is
+// issued as soon as the last earlier load whose place overlaps its own (counting back through
+// the previous tile's loads) has been consumed: `dep` loads back.  The two full-halo boxes take
+// the two halves, as two plain buffers would, but the small boxes (10-32 KB) share a half and
+// their copies start two to three phases ahead instead of one.  Each load has its own mbarrier,
+// which completes once per tile.
+constexpr int kRingElems = 2 * kBufElems;
+struct RingPlan {
+    int off[kLoads];
+    int dep[kLoads];
+    bool ok;
+};
+constexpr RingPlan ring_plan() {
+    RingPlan r{{0, 10240, 0, 10240, 0, 10240, 0, 10240, 12800, 0, 4096, 6656, 10752, 0, 5120, 9216, 14336, 0, 4096, 8192},
+               {},
+               true};
+    for (int e = 0; e < kLoads; e++) {
+        const int a0 = r.off[e], a1 = a0 + box_elems(kSchedPlan[e].shape);
+        if (a0 < 0 || a0 % 128 != 0 || a1 > kRingElems) r.ok = false;
+        r.dep[e] = kLoads;  // a load always overlaps its own place in the previous tile
+        for (int back = kLoads - 1; back >= 1; back--) {
+            const int q = (e - back + kLoads) % kLoads;
+            const int b0 = r.off[q], b1 = b0 + box_elems(kSchedPlan[q].shape);
+            if (b0 < a1 && a0 < b1) r.dep[e] = back;
+        }
+    }
+    return r;
+}
+static_assert(ring_plan().ok, "every load lies inside the ring at a 512-byte boundary");
+__constant__ RingPlan kRing = ring_plan();
 
 template <int STAGE>
 __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __restrict__ boxes,
                                                             const Tile* __restrict__ tiles, int ntiles) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* buf = (float*)smem_raw;                                // kWsBufs field buffers
-    float* stash = buf + kWsBufs * kBufElems;                     // kWsSlots stash slots
-    uint64_t* bar = (uint64_t*)(stash + kWsSlots * kStashElems);  // TMA[kWsBufs], full[kWsSlots], empty[kWsSlots]
-    uint64_t* full = bar + kWsBufs;
+    float* buf = (float*)smem_raw;                                // the field ring
+    float* stash = buf + kRingElems;                              // kWsSlots stash slots
+    uint64_t* bar = (uint64_t*)(stash + kWsSlots * kStashElems);  // TMA[kLoads], full[kWsSlots], empty[kWsSlots]
+    uint64_t* full = bar + kLoads;
     uint64_t* empty = full + kWsSlots;
     const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     if (my_tiles <= 0) return;
     if (threadIdx.x == 0) {
-        for (int q = 0; q < kWsBufs; q++) mbar_init(&bar[q]);
+        for (int q = 0; q < kLoads; q++) mbar_init(&bar[q]);
         for (int q = 0; q < kWsSlots; q++) {
             mbar_init_n(&full[q], kTileThreads);
             mbar_init_n(&empty[q], kTileThreads);
@@ -1049,13 +1082,16 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
     // ---- stencil group
     const int tid = threadIdx.x, tk = tid & (XK - 1), tj = tid >> 5;
     const int total = my_tiles * kLoads;
-    auto issue_load = [&](int l) {  // load l of this block into buffer l % kWsBufs
-        const int nt = blockIdx.x + (l / kLoads) * gridDim.x;
-        issue(boxes, tiles, nt, l % kLoads, flip, buf + (l % kWsBufs) * kBufElems, &bar[l % kWsBufs]);
+    // thread 0: issue, in order, every load whose place in the ring is free once the loads up to
+    // `consumed` have been consumed
+    int issued = 0;  // loads issued so far
+    auto issue_ready = [&](int consumed) {
+        for (; issued < total && issued - kRing.dep[issued % kLoads] <= consumed; issued++) {
+            const int e = issued % kLoads, nt = blockIdx.x + (issued / kLoads) * gridDim.x;
+            issue(boxes, tiles, nt, e, flip, buf + kRing.off[e], &bar[e]);
+        }
     };
-    int issued = 0;  // thread 0: loads issued so far
-    if (tid == 0)
-        for (; issued < kWsBufs - 1 && issued < total; issued++) issue_load(issued);
+    if (tid == 0) issue_ready(-1);
     bool bad = false;
     int* bad_status = nullptr;  // the status word of the box whose wait gave up
     int g = 0;
@@ -1070,14 +1106,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
 #pragma unroll
         for (int i = 0; i < XI; i++) dmx[i] = dmy[i] = dmz[i] = de[i] = f0[i] = c0[i] = 0.f;
         for (int e = 0; e < kLoads; e++, g++) {
-            // buffer (g + kWsBufs - 1) % kWsBufs held load g - 1, consumed before the last barrier
-            if (tid == 0 && !bad && issued < total && issued <= g + kWsBufs - 1) issue_load(issued++);
-            if (!bad && !mbar_wait_bounded(&bar[g % kWsBufs], (uint32_t)((g / kWsBufs) & 1))) {
+            // loads up to g - 1 were consumed before the last barrier
+            if (tid == 0 && !bad) issue_ready(g - 1);
+            if (!bad && !mbar_wait_bounded(&bar[e], (uint32_t)(it & 1))) {
                 bad = true;
                 bad_status = &b.sc->status;
             }
-            if (!bad) consume_field(e, buf + (g % kWsBufs) * kBufElems, T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
-            group_sync();  // buffer g % kWsBufs is free for load g + kWsBufs
+            if (!bad) consume_field(e, buf + kRing.off[e], T, b, cf, tj, tk, dmx, dmy, dmz, de, f0, c0);
+            group_sync();  // load g's place in the ring is free
         }
         // hand the sums over: slot it % kWsSlots, once the write-back of tile it - kWsSlots has released it
         const int slot = it % kWsSlots;
@@ -1090,9 +1126,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_assemble_ws(const BoxView* __
     }
     if (bad) {
         atomicOr(bad_status, HEALTH_TIMEOUT);
-        if (tid == 0)  // the copies still in flight are among the last ones issued
-            for (int l = max(0, issued - kWsBufs); l < issued; l++)
-                mbar_wait_bounded(&bar[l % kWsBufs], (uint32_t)((l / kWsBufs) & 1));
+        if (tid == 0)  // the copies still in flight are among the last kLoads issued
+            for (int l = max(0, issued - kLoads); l < issued; l++)
+                mbar_wait_bounded(&bar[l % kLoads], (uint32_t)((l / kLoads) & 1));
     }
 }
 
@@ -1383,7 +1419,7 @@ cudaError_t launch_deriv_tma(const BoxView* boxes, const Tile* tiles, int ntiles
 }
 
 constexpr size_t kWsSmem =
-    (kWsBufs * kBufElems + kWsSlots * kStashElems) * sizeof(float) + (kWsBufs + 2 * kWsSlots) * sizeof(uint64_t);
+    (kRingElems + kWsSlots * kStashElems) * sizeof(float) + (kLoads + 2 * kWsSlots) * sizeof(uint64_t);
 
 template <int STAGE>
 static cudaError_t launch_ws_stage(const BoxView* boxes, const Tile* tiles, int ntiles, cudaStream_t st) {
