@@ -128,9 +128,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
                 const double r = (double)f[l];
                 if (STAGE == 1) {
                     un[l] = fma(dt, r, b.U[e]);
-                    b.Us[e] = un[l];
+                    b.Us[e] = sizeof(R) == 4 ? quarter(un[l]) : un[l];  // mixed boxes keep U1 / 4
                 } else if (STAGE == 2) {
-                    un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                    un[l] = sizeof(R) == 4 ? fma(0.75, b.U[e], fma(0.25 * dt, r, b.Us[e]))
+                                           : fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
                     b.Us[e] = un[l];
                 } else {
                     un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));

@@ -606,11 +606,24 @@ __device__ __forceinline__ float courant_mixed_est(const BoxView& b, float rf, f
     return fmaxf(fmaxf(cx, cy), cz);
 }
 
-// What a write-back that defers the FP64 Courant number keeps of a cell: the estimate and p.
+// What a write-back that defers the FP64 Courant number keeps of a cell: the estimate and
+// p - p_ref (the FP64 number is formed from p = (p - p_ref) + p_ref only for candidates).
 struct CourantInput {
     float est;
-    double p;
+    double pd;
 };
+
+// x / 4, exactly, on the integer pipes (the exponent field lowered by two) for normal x of
+// exponent field >= 3; infinities and NaNs stay as they are and values below 2^-1020 become a
+// zero of their sign.  The mixed form keeps its first RK3 stage as U1 / 4, so that the second
+// stage's 0.25 (U1 + dt L) is one FMA, fma(dt / 4, L, U1 / 4), with the same bits.
+__device__ __forceinline__ double quarter(double x) {
+    const long long bits = __double_as_longlong(x);
+    const unsigned ef = (unsigned)(bits >> 52) & 0x7FFu;
+    const long long q =
+        ef >= 3u ? (ef == 0x7FFu ? bits : bits - (2ll << 52)) : (long long)((unsigned long long)bits & (1ull << 63));
+    return __longlong_as_double(q);
+}
 
 __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
                                                  int k, const double un[5], bool want_cour, int* health,
@@ -628,24 +641,29 @@ __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __rest
     const float rf = 1.0f / rhof;
     const float mx = (float)un[1], my = (float)un[2], mz = (float)un[3];
     const float u = mx * rf, v = my * rf, w = mz * rf;
-    // E/rho to ~1e-15 in FP64 from the FP32 reciprocal: y0 = E r, y = y0 + (E - rho y0) r
-    const double r64 = (double)rf;
-    const double y0 = E * r64;
-    const double erho = fma(fma(-rho, y0, E), r64, y0);
-    const float ke = fmaf(u, u, fmaf(v, v, w * w));
-    const double eint = fma(-0.5, (double)ke, erho);  // the cancelling subtraction, in FP64
-    // offsets from the box's reference values, formed in FP64 before rounding to FP32
-    const double pd = fma(kGm1 * rho, eint, -sc.p);        // p - p_ref
+    // rho e = E - rho |u|^2 / 2: the cancelling subtraction in FP64, with the kinetic energy
+    // density rho |u|^2 / 2 formed in FP32 (cpu/ctoprim.cpp's E/rho - |u|^2/2, times rho)
+    const float kd = 0.5f * fmaf(mx, u, fmaf(my, v, mz * w));
+    const double re = E - (double)kd;
+    // offsets from the box's reference values, formed in FP64 before rounding to FP32:
+    // p - p_ref = (gamma - 1) rho e - p_ref, and e - e_ref (= c_v (T - T_ref)) as
+    // (rho e - rho e_ref) / rho, the difference in FP64 and the division in FP32
+    const double pd = fma(kGm1, re, -sc.p);
     const float dp = (float)pd;
-    const float dT = (float)(eint - sc.e);                  // e - e_ref (= c_v (T - T_ref))
-    const float dH = (float)(E - sc.E) + dp;                // (E + p) - H_ref
-    *health |= health_bits(rho, eint);
+    const float dT = (float)fma(-rho, sc.e, re) * rf;
+    const float dH = (float)(E - sc.E) + dp;  // (E + p) - H_ref
+    // rho e has the sign and finiteness of e where rho > 0 (elsewhere rho's own bit is set)
+    *health |= health_bits(rho, re);
     const float pv[NPF] = {u, v, w, dT, mx, my, mz, fmaf(mx, u, dp), fmaf(my, v, dp), fmaf(mz, w, dp),
                            mx * v, mx * w, my * w, dH * u, dH * v, dH * w};
     store_pset(Pw, b, c, i, j, k, pv);
     if (ci) {
-        ci->p = pd + sc.p;
-        ci->est = courant_mixed_est(b, rf, u, v, w, (float)ci->p);
+        // the estimate's p in FP32 as (p - p_ref) + p_ref: within 5 * 2^-24 of p while p >= p_ref / 2
+        // (three roundings of at most 2p each), which keeps the estimate's bound; cells below
+        // that are left to the FP64 number (a NaN estimate always makes a cell a candidate)
+        const float pref = (float)sc.p;
+        ci->pd = pd;
+        ci->est = dp >= -0.5f * pref ? courant_mixed_est(b, rf, u, v, w, dp + pref) : __int_as_float(0x7FC00000);
     }
     if (!want_cour) return 0.0;
     return courant_mixed(b, rho, un[1], un[2], un[3], pd + sc.p);

@@ -422,7 +422,7 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
                                            int tk) {
     const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
     float* Pw = (float*)b.P[pr ^ 1];
-    const double dt = b.sc->dt;
+    const double dt = b.sc->dt, dt4 = 0.25 * dt;
     const MixedRefs refs = mixed_refs(b);
     const int j = T.j0 + tj, k = T.k0 + tk;
     const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
@@ -470,9 +470,9 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
             const double r = (double)f[l];
             if (STAGE == 1) {
                 un[l] = fma(dt, r, u0[l]);
-                b.Us[e] = un[l];
+                b.Us[e] = quarter(un[l]);  // U1 / 4
             } else if (STAGE == 2) {
-                un[l] = fma(0.75, u0[l], 0.25 * fma(dt, r, us[l]));
+                un[l] = fma(0.75, u0[l], fma(dt4, r, us[l]));  // = fma(0.75, U0, 0.25 * fma(dt, L, U1))
                 b.Us[e] = un[l];
             } else {
                 un[l] = fma(1.0 / 3.0, u0[l], (2.0 / 3.0) * fma(dt, r, us[l]));
@@ -481,12 +481,12 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
         }
         if (STAGE == 3) {
             if (b.host_out) store_host(b, ic, j, k, un);
-            // park the FP32 Courant estimate and p (FP64, as two words) over the cell's sums
+            // park the FP32 Courant estimate and p - p_ref (FP64, as two words) over the cell's sums
             CourantInput ci;
             epilogue_mixed(b, Pw, c, ic, j, k, un, false, &health, refs, &ci);
             stash[(i * 5 + 0) * kTileThreads + col] = ci.est;
-            stash[(i * 5 + 1) * kTileThreads + col] = __int_as_float(__double2hiint(ci.p));
-            stash[(i * 5 + 2) * kTileThreads + col] = __int_as_float(__double2loint(ci.p));
+            stash[(i * 5 + 1) * kTileThreads + col] = __int_as_float(__double2hiint(ci.pd));
+            stash[(i * 5 + 2) * kTileThreads + col] = __int_as_float(__double2loint(ci.pd));
             m32 = fmaxf(m32, ci.est);
         } else {
             epilogue_mixed(b, Pw, c, ic, j, k, un, false, &health, refs);
@@ -519,7 +519,8 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
                 cand &= cand - 1;
                 const long long c = cell_off(b, T.i0 + i, j, k);
                 const double p = __hiloint2double(__float_as_int(stash[(i * 5 + 1) * kTileThreads + col]),
-                                                  __float_as_int(stash[(i * 5 + 2) * kTileThreads + col]));
+                                                  __float_as_int(stash[(i * 5 + 2) * kTileThreads + col])) +
+                                 refs.p;
                 const double cour = courant_mixed(b, b.U[c], b.U[c + fs], b.U[c + 2 * fs], b.U[c + 3 * fs], p);
                 cmax = cour > cmax ? cour : cmax;
             }
