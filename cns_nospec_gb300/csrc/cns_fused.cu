@@ -132,9 +132,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
                 } else if (STAGE == 2) {
                     un[l] = sizeof(R) == 4 ? fma(0.75, b.U[e], fma(0.25 * dt, r, b.Us[e]))
                                            : fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
-                    b.Us[e] = un[l];
+                    b.Us[e] = sizeof(R) == 4 ? (2.0 / 3.0) * un[l] : un[l];  // mixed: (2/3) U2
                 } else {
-                    un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
+                    un[l] = sizeof(R) == 4 ? fma(1.0 / 3.0, b.U[e], fma((2.0 / 3.0) * dt, r, b.Us[e]))
+                                           : fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
                     b.U[e] = un[l];
                 }
             }

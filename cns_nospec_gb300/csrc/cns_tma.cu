@@ -422,7 +422,7 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
                                            int tk) {
     const int pr = b.sc->pbase ^ ((STAGE - 1) & 1);
     float* Pw = (float*)b.P[pr ^ 1];
-    const double dt = b.sc->dt, dt4 = 0.25 * dt;
+    const double dt = b.sc->dt, dt4 = 0.25 * dt, dt23 = (2.0 / 3.0) * dt;
     const MixedRefs refs = mixed_refs(b);
     const int j = T.j0 + tj, k = T.k0 + tk;
     const int jc = min(j, b.n[1] - 1), kc = min(k, b.n[2] - 1);
@@ -473,9 +473,9 @@ __device__ __forceinline__ void write_back(const BoxView& b, const Tile& T, floa
                 b.Us[e] = quarter(un[l]);  // U1 / 4
             } else if (STAGE == 2) {
                 un[l] = fma(0.75, u0[l], fma(dt4, r, us[l]));  // = fma(0.75, U0, 0.25 * fma(dt, L, U1))
-                b.Us[e] = un[l];
+                b.Us[e] = (2.0 / 3.0) * un[l];  // (2/3) U2
             } else {
-                un[l] = fma(1.0 / 3.0, u0[l], (2.0 / 3.0) * fma(dt, r, us[l]));
+                un[l] = fma(1.0 / 3.0, u0[l], fma(dt23, r, us[l]));  // U0 / 3 + (2/3) (U2 + dt L)
                 b.U[e] = un[l];
             }
         }
