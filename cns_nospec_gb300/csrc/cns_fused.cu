@@ -128,10 +128,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_assemble(const BoxView* __r
                 const double r = (double)f[l];
                 if (STAGE == 1) {
                     un[l] = fma(dt, r, b.U[e]);
-                    b.Us[e] = sizeof(R) == 4 ? quarter(un[l]) : un[l];  // mixed boxes keep U1 / 4
+                    b.Us[e] = quarter(un[l]);  // U1 / 4
                 } else if (STAGE == 2) {
-                    un[l] = sizeof(R) == 4 ? fma(0.75, b.U[e], fma(0.25 * dt, r, b.Us[e]))
-                                           : fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                    un[l] = fma(0.75, b.U[e], fma(0.25 * dt, r, b.Us[e]));
                     b.Us[e] = sizeof(R) == 4 ? (2.0 / 3.0) * un[l] : un[l];  // mixed: (2/3) U2
                 } else {
                     un[l] = sizeof(R) == 4 ? fma(1.0 / 3.0, b.U[e], fma((2.0 / 3.0) * dt, r, b.Us[e]))

@@ -557,9 +557,9 @@ __device__ __forceinline__ void write_back_plain(const BoxView& b, const Tile& T
             const double r = stash[(i * 5 + l) * kTileThreads + col];
             if (STAGE == 1) {
                 un[l] = fma(dt, r, b.U[e]);
-                b.Us[e] = un[l];
+                b.Us[e] = quarter(un[l]);  // U1 / 4
             } else if (STAGE == 2) {
-                un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                un[l] = fma(0.75, b.U[e], fma(0.25 * dt, r, b.Us[e]));
                 b.Us[e] = un[l];
             } else {
                 un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
@@ -852,9 +852,9 @@ __device__ __forceinline__ void write_back_fx(const BoxView& b, const Tile& T, d
             const double r = stash[(i * 5 + l) * kTileThreads + col];
             if (STAGE == 1) {
                 un[l] = fma(dt, r, b.U[e]);
-                b.Us[e] = un[l];
+                b.Us[e] = quarter(un[l]);  // U1 / 4
             } else if (STAGE == 2) {
-                un[l] = fma(0.75, b.U[e], 0.25 * fma(dt, r, b.Us[e]));
+                un[l] = fma(0.75, b.U[e], fma(0.25 * dt, r, b.Us[e]));
                 b.Us[e] = un[l];
             } else {
                 un[l] = fma(1.0 / 3.0, b.U[e], (2.0 / 3.0) * fma(dt, r, b.Us[e]));
