@@ -61,6 +61,19 @@ __host__ __device__ __forceinline__ int xclz64(unsigned long long x) {
 #endif
 }
 
+// x / 4, exactly, on the integer pipes (the exponent field lowered by two) for normal x of
+// exponent field >= 3; infinities and NaNs stay as they are and values below 2^-1020 become a
+// zero of their sign.  Both forms keep the first RK3 stage as U1 / 4, so that the second stage's
+// 0.25 (U1 + dt L) is one FMA, fma(dt / 4, L, U1 / 4), with the same bits.  The mixed form keeps
+// its second stage as (2/3) U2, so that the third stage's (2/3) (U2 + dt L) is
+// fma(2 dt / 3, L, (2/3) U2): the multiply moves from stage 3, whose write-back also forms the
+// Courant maximum, to stage 2.
+__host__ __device__ __forceinline__ double quarter(double x) {
+    const unsigned long long bits = ((unsigned long long)(unsigned)xhi(x) << 32) | xlo(x);
+    const unsigned ef = (unsigned)(bits >> 52) & 0x7FFu;
+    return xbits(ef >= 3u ? (ef == 0x7FFu ? bits : bits - (2ull << 52)) : (bits & (1ull << 63)));
+}
+
 constexpr int kXGuard = 9;  // guard bits below the largest tap's ulp
 
 // Which stencils of the plain form take the exact sums (the others the FP64 chain), as masks

@@ -613,21 +613,6 @@ struct CourantInput {
     double pd;
 };
 
-// x / 4, exactly, on the integer pipes (the exponent field lowered by two) for normal x of
-// exponent field >= 3; infinities and NaNs stay as they are and values below 2^-1020 become a
-// zero of their sign.  Both forms keep the first RK3 stage as U1 / 4, so that the second stage's
-// 0.25 (U1 + dt L) is one FMA, fma(dt / 4, L, U1 / 4), with the same bits.  The mixed form keeps
-// its second stage as (2/3) U2, so that the third stage's (2/3) (U2 + dt L) is
-// fma(2 dt / 3, L, (2/3) U2): the multiply moves from stage 3, whose write-back also forms the
-// Courant maximum, to stage 2.
-__device__ __forceinline__ double quarter(double x) {
-    const long long bits = __double_as_longlong(x);
-    const unsigned ef = (unsigned)(bits >> 52) & 0x7FFu;
-    const long long q =
-        ef >= 3u ? (ef == 0x7FFu ? bits : bits - (2ll << 52)) : (long long)((unsigned long long)bits & (1ull << 63));
-    return __longlong_as_double(q);
-}
-
 __device__ __forceinline__ double epilogue_mixed(const BoxView& b, float* __restrict__ Pw, long long c, int i, int j,
                                                  int k, const double un[5], bool want_cour, int* health,
                                                  const MixedRefs& sc, CourantInput* ci = nullptr);
