@@ -536,8 +536,8 @@ def run_ours(args, dist):
         "form": {"plain": "FP64 (CNS_ASSEMBLE_FX); of the 39 8-tap stencil sums per cell and stage, the 21 of the "
                           "derivative pass and the Laplacians are exact integer sums of 62-bit fixed-point copies of "
                           "u, v, w, e (on cubic cells the second differences of a field that share a factor in one "
-                          "sum) and the 5 k-axis flux divergences exact integer sums of the FP64 significands, each "
-                          "sum rounded once to FP64; the other 13 FP64 chains",
+                          "sum) and the 5 k-axis flux divergences and the k-axis mixed viscous term exact integer "
+                          "sums of the FP64 significands, each sum rounded once to FP64; the other 12 FP64 chains",
                  "plain_kernel": {C.CNS_ASSEMBLE_FX: "fx", C.CNS_ASSEMBLE_DIRECT: "direct"}.get(f64["kernel"], "other"),
                  "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 box",
                  "tile_log2_ijk": {"fp64": list(f64["tile"]), "mixed": list(mix["tile"])},

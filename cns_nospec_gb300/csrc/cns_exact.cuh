@@ -80,7 +80,7 @@ constexpr int kXGuard = 9;  // guard bits below the largest tap's ulp
 // over the axes (bit d: along d): the first derivatives of the derivative pass, those of the
 // flux divergence, those of the mixed viscous terms, the Laplacian second differences.  The
 // integer and FP64 pipes work side by side, so the best split keeps both busy.
-constexpr int kExactDeriv = 0b110, kExactFlux = 0b100, kExactMixed = 0, kExactLap = 0b110;
+constexpr int kExactDeriv = 0b110, kExactFlux = 0b100, kExactMixed = 0b100, kExactLap = 0b110;
 constexpr bool xon(int mask, int axis) { return (mask >> axis) & 1; }
 
 // The exponent field (bits 20-30 of the high word) of the largest of a set of taps, at least 1
