@@ -1244,9 +1244,9 @@ static int upload_first_step(cns_box* b, double* h_map, bool ghosts) {
     if (!b->d_counters) CK(cudaMalloc((void**)&b->d_counters, sizeof(int) * (b->desc.n[0] + 1)));
     CK(cudaMemsetAsync(b->d_sc, 0, sizeof(BoxScalars), b->stream));
     CK(host_upload_deriv(b->view, h_map, ghosts, b->d_tiles, b->d_queue, b->nq, b->d_counters, b->stream));
-    // (no k_refs: the FP64 form does not use the mixed form's reference values)
-    int rc = fx_after_upload(b, false);
-    if (rc) return rc;
+    // (no k_refs: the FP64 form does not use the mixed form's reference values; the upload
+    // also formed the maxima of the fields with copies, so only the copy pass is left)
+    if (b->view.fx) CK(launch_fx_pass(true, b->d_view, b->d_tiles, b->ntiles, b->stream));
     CK(launch_stepend(b->d_view, 1, 0, b->stream));
     b->primed = true;
     return enqueue_step(b->d_view, 1, box_lists(b), b->stream, nullptr, nullptr, true);

@@ -192,6 +192,8 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_upload_deriv(BoxView b, doub
     __shared__ double s[kWarps][kRun * CNS_NC];
     __shared__ int s_item, s_ok;
     __shared__ float s_max[kWarps];
+    __shared__ int s_emax[NPF];  // boxes with fixed-point copies: the block's P-field maxima
+    if (threadIdx.x < NPF) s_emax[threadIdx.x] = 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double* sw = s[warp];
     const int runs = (b.n[2] + kRun - 1) / kRun, per_plane = b.n[1] * runs;
@@ -205,7 +207,11 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_upload_deriv(BoxView b, doub
         __syncthreads();
         const int item = s_item;
         __syncthreads();  // s_item is rewritten next round
-        if (item == INT_MIN) return;
+        if (item == INT_MIN) {
+            // the maxima of the fields with copies, for the copies' exponents (k_fx_pass<true>)
+            if (threadIdx.x < b.fx && s_emax[threadIdx.x] > 0) atomicMax(&b.sc->fx_cur[threadIdx.x], s_emax[threadIdx.x]);
+            return;
+        }
         if (item >= 0) {  // upload: run (item % items_per_plane) * 8 + warp of plane order q
             const int q = item / items_per_plane, rr = (item % items_per_plane) * kWarps + warp;
             const bool has = rr < per_plane;  // warp-uniform; warps without a run still join the barriers
@@ -231,8 +237,10 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_upload_deriv(BoxView b, doub
                     un[l] = sw[lane * CNS_NC + l];
                     b.U[c + l * b.fs] = un[l];
                 }
-                epilogue_plain(b, (double*)b.P[b.sc->pbase], c, r.i, r.j, k, un, &health, &cq);
+                double* P = (double*)b.P[b.sc->pbase];
+                epilogue_plain(b, P, c, r.i, r.j, k, un, &health, &cq);
                 est = courant_plain_est(b, cq);
+                for (int f = 0; f < b.fx; f++) fx_track(s_emax + f, fx_efield(P[f * b.fs + c]));
             }
             // The Courant maximum through FP32 candidates over the item's 8 runs, as in stage 3
             // of k_assemble: the FP64 number only where it can be the largest, bit for bit.
